@@ -1,0 +1,377 @@
+#!/usr/bin/env python3
+"""Benchmark of the WAH index build on GB300.
+
+Default workload (one GPU): one column of 268,435,456 uint32 values, i.i.d.
+uniform in [0, 65535] from a seeded PRNG (numpy PCG64), bound = 65535 (the
+reference's -b).  A step is one full index build of that column: digit
+histogram, plan, two onesweep digit passes, fused index build.
+
+Printed: one JSON line on stdout.  Per-phase "N us" lines (the reference's
+SHOW_TIME_CONSUMPTION output, src/phases.cpp:714-1127) go to stderr.
+
+  value       rows/s with the column resident in HBM (CUDA events around K
+              builds on the launching stream; the 1 GiB input and 6+ GiB of
+              traffic per build exceed the 129 MB L2, so no flush is needed)
+  e2e         rows/s through wah_ctx_build_host with pinned host buffers:
+              H2D of the values, build, D2H of keys/offsets/index, per step
+  roofline    the dominant kernel's algorithmic bytes / its mean event-timed
+              duration, against the measured HBM copy bandwidth
+  cpu_baseline  the oracle (plain-C restatement of the reference `cpu`
+              program) on a bounded sample, host cores of this machine
+
+--impl reference times the reference CPU implementation (the oracle port:
+the reference's own sources are not on the GPU machine) on all host threads.
+Multi-GPU (torchrun): independent replicas, one column per rank, no
+collective on the data path ("scaling": "weak").
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+METRIC = "rows/s & HBM GB/s at 256M u32; batched rows/s + p50/p99 vs plain, bit-exact"
+PHASES = ["histogram", "plan", "pass0", "pass1", "pass2", "pass3", "build"]
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n", type=int, default=268_435_456)
+    ap.add_argument("--card", type=int, default=65536, help="values uniform in [0, card)")
+    ap.add_argument("--seed", type=int, default=20170101)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-sample", type=int, default=1 << 23,
+                    help="rows per oracle build in the CPU legs")
+    return ap.parse_args()
+
+
+def gen_uniform(n: int, card: int, seed: int) -> np.ndarray:
+    return np.random.default_rng(seed).integers(0, card, size=n, dtype=np.uint32)
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled every 200 ms while running."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.t.join(timeout=2)
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, val in zip(names, f[5:9]):
+                if val.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_oracle_rate(values: np.ndarray, sample: int, threads: int, repeats: int):
+    """Oracle builds of `threads` disjoint slices of `sample` rows, in parallel
+    (ctypes releases the GIL).  Returns rows/s and the wall time."""
+    from oracle import oracle as O
+    O._load()
+    slices = [values[(i * sample) % max(values.size - sample + 1, 1):][:sample]
+              for i in range(threads)]
+    t0 = time.perf_counter()
+    for _ in range(repeats):
+        ths = [threading.Thread(target=O.build, args=(s,)) for s in slices]
+        for t in ths:
+            t.start()
+        for t in ths:
+            t.join()
+    dt = time.perf_counter() - t0
+    return threads * sample * repeats / dt, dt
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    O.make()
+    n = args.n
+    card = args.card
+    values = gen_uniform(min(n, max(args.cpu_sample * 4, 1 << 22)), card, args.seed)
+    threads = os.cpu_count() or 1
+    sample = min(args.cpu_sample, values.size)
+    for _ in range(max(args.warmup, 0)):
+        cpu_oracle_rate(values, sample, threads, 1)
+    times = []
+    for _ in range(args.steps):
+        r, dt = cpu_oracle_rate(values, sample, threads, 1)
+        times.append(dt)
+    total = sum(times)
+    rate = threads * sample * args.steps / total
+    line = {
+        "impl": "reference", "metric": METRIC, "value": rate, "unit": "rows/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "config": {"workload": f"one column, {n} uint32 uniform [0,{card - 1}], seed "
+                               f"{args.seed}", "rows": n, "bound": card - 1},
+        "cpu_baseline": {"value": rate, "unit": "rows/s", "cores": threads, "kind": "port",
+                         "sample": f"{threads} threads x one oracle build each of {sample} "
+                                   f"rows (disjoint slices of the seeded column) per step"},
+        "e2e": {"value": rate, "unit": "rows/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+
+    import torch
+    import indexing_gb300 as wah
+    from indexing_gb300 import _lib
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+
+    lib = _lib.load()
+    n, card = args.n, args.card
+    bound = card - 1
+    values_np = gen_uniform(n, card, args.seed + rank)
+    d_values = torch.from_numpy(values_np.view(np.int32)).to(dev)
+    bufs = wah._Buffers(n, bound, dev)
+    stream = torch.cuda.current_stream(dev)
+    sh = stream.cuda_stream
+
+    def step(events=None):
+        if events is None:
+            rc = lib.wah_build(d_values.data_ptr(), n, bound, bufs.keys.data_ptr(),
+                               bufs.offsets.data_ptr(), bufs.index.data_ptr(),
+                               bufs.counts.data_ptr(), bufs.ws.data_ptr(), bufs.ws_bytes, sh)
+        else:
+            rc = lib.wah_build_timed(d_values.data_ptr(), n, bound, bufs.keys.data_ptr(),
+                                     bufs.offsets.data_ptr(), bufs.index.data_ptr(),
+                                     bufs.counts.data_ptr(), bufs.ws.data_ptr(), bufs.ws_bytes,
+                                     sh, events)
+        if rc != 0:
+            raise wah.WahError(rc, "wah_build")
+
+    # Per-phase events for every timed step (recorded on the build's stream).
+    n_ev = 2 * len(PHASES)
+    ev_arrays = []
+    for _ in range(args.steps):
+        arr = (ctypes.c_void_p * n_ev)()
+        if lib.wah_events_create(n_ev, arr) != 0:
+            raise RuntimeError("event creation failed")
+        ev_arrays.append(arr)
+
+    with ClockSampler(local) as clocks:
+        for _ in range(args.warmup):
+            step()
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        t_start = torch.cuda.Event(enable_timing=True)
+        t_end = torch.cuda.Event(enable_timing=True)
+        launches = 0
+        t_start.record(stream)
+        for i in range(args.steps):
+            step(ev_arrays[i])
+            launches += wah.last_launch_count()
+        t_end.record(stream)
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+    elapsed_ms = t_start.elapsed_time(t_end)
+    c = bufs.counts.cpu().numpy().view(np.uint32)
+    if c[3] != 0:
+        raise wah.WahError(int(c[3]), "wah_build (device)")
+    K, L, k = int(c[0]), int(c[1]), int(c[2])
+
+    # per-phase mean durations over the timed steps
+    phase_ms = {p: 0.0 for p in PHASES}
+    f = ctypes.c_float()
+    for arr in ev_arrays:
+        for j, p in enumerate(PHASES):
+            lib.wah_events_elapsed(arr[2 * j], arr[2 * j + 1], ctypes.byref(f))
+            phase_ms[p] += f.value / args.steps
+    for arr in ev_arrays:
+        lib.wah_events_destroy(n_ev, arr)
+
+    max_ms = elapsed_ms
+    if dist:
+        t = torch.tensor([elapsed_ms], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        max_ms = float(t.item())
+    ms_per_step = max_ms / args.steps
+    value = world * n * args.steps / (max_ms / 1e3)
+
+    # Algorithmic bytes (per build; integer keys <= 16 bits -> 2 digit passes):
+    #   histogram 4n, pass0 12n (read key, write key+rid), pass1 16n,
+    #   build 8n + 4L + 8K (read sorted key+rid, write words, keys, offsets)
+    alg = {"histogram": 4 * n, "plan": 0, "pass0": 12 * n, "pass1": 16 * n, "pass2": 0,
+           "pass3": 0, "build": 8 * n + 4 * L + 8 * K}
+    per_unit = {"histogram": "4 B/row", "pass0": "12 B/row", "pass1": "16 B/row",
+                "build": "8 B/row + 4 B/word + 8 B/key"}
+    dom = max(PHASES, key=lambda p: phase_ms[p])
+    peak, peak_kind = load_peaks()
+    ach = alg[dom] / (phase_ms[dom] / 1e3) / 1e9 if phase_ms[dom] > 0 else 0.0
+    total_alg = sum(alg.values())
+    for p in PHASES:
+        if rank == 0:
+            gbs = alg[p] / (phase_ms[p] / 1e3) / 1e9 if phase_ms[p] > 0 and alg[p] else 0
+            print(f"{p}:\t{phase_ms[p] * 1e3:.0f} us\t{gbs:.0f} GB/s", file=sys.stderr)
+
+    # End to end: host values in, host index out, through the C ABI context.
+    e2e = None
+    if not args.no_e2e:
+        pin_v = torch.empty(n, dtype=torch.int32, pin_memory=True)
+        pin_v.numpy()[:] = values_np.view(np.int32)
+        kc, ic = wah.output_caps(n, bound)
+        pin_k = torch.empty(kc, dtype=torch.int32, pin_memory=True)
+        pin_o = torch.empty(kc, dtype=torch.int32, pin_memory=True)
+        pin_i = torch.empty(ic, dtype=torch.int32, pin_memory=True)
+        del bufs  # free the device-resident run's buffers
+        torch.cuda.empty_cache()
+        ctx = wah.HostContext(n, bound)
+        cnt = wah.wah_counts()
+        e2e_steps = max(3, min(args.steps, 20))
+
+        def e2e_step():
+            rc = lib.wah_ctx_build_host(ctx._h, pin_v.data_ptr(), n, pin_k.data_ptr(),
+                                        pin_o.data_ptr(), pin_i.data_ptr(), ctypes.byref(cnt))
+            if rc != 0:
+                raise wah.WahError(rc, "wah_ctx_build_host")
+
+        for _ in range(max(1, args.warmup)):
+            e2e_step()
+        if dist:
+            dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            e2e_step()
+        dt = time.perf_counter() - t0
+        if dist:
+            t = torch.tensor([dt], device=dev, dtype=torch.float64)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            dt = float(t.item())
+        assert cnt.keycnt == K and cnt.index_len == L
+        e2e = {"value": world * n * e2e_steps / dt, "unit": "rows/s",
+               "h2d_bytes_per_step": 4 * n,
+               "d2h_bytes_per_step": 16 + 8 * cnt.keycnt + 4 * cnt.index_len,
+               "ms_per_step": 1e3 * dt / e2e_steps, "steps": e2e_steps}
+        ctx.close()
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        sample = min(args.cpu_sample, n)
+        rate, dt = cpu_oracle_rate(values_np, sample, 1, 1)
+        reps = max(1, min(5, int(10.0 / max(dt, 1e-3))))
+        if reps > 1:
+            rate, dt = cpu_oracle_rate(values_np, sample, 1, reps)
+        cpu = {"value": rate, "unit": "rows/s", "cores": 1, "kind": "port",
+               "sample": f"{reps} oracle build(s) of the first {sample} rows of the same "
+                         f"column, 1 thread ({dt:.1f} s)"}
+
+    if rank == 0:
+        cl = clocks.summary()
+        line = {
+            "metric": METRIC, "value": value, "unit": "rows/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "u32", "data": "synthetic",
+            "config": {"workload": f"plain method, one column of {n} uint32 i.i.d. uniform "
+                                   f"[0,{card - 1}] (seed {args.seed}+rank), bound {bound}",
+                       "rows": n, "bound": bound, "parallelism": f"replicas x{world}",
+                       "l2": "inputs larger than L2 (1 GiB column), no flush"},
+            "outputs": {"keycnt": K, "index_len": L, "merged": k},
+            "hbm_gbs_pipeline": total_alg / (ms_per_step / 1e3) / 1e9,
+            "phase_us": {p: round(phase_ms[p] * 1e3, 1) for p in PHASES},
+            "roofline": {"bound": "hbm", "kernel": dom, "per_unit": per_unit.get(dom),
+                         "achieved": ach, "peak": peak, "unit": "GB/s",
+                         "frac": ach / peak, "peak_kind": peak_kind, "traffic": None},
+            "gpu_launches": launches,
+            "clocks": cl,
+            "e2e": e2e,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,161 @@
+/*
+ * wah.h -- C ABI of the GB300 WAH bitmap index builder.
+ *
+ * One call builds the WAH bitmap index of a uint32 column on the GPU:
+ *   keys[K]     the distinct values, ascending
+ *   offsets[K]  position of each key's first word in index (u32)
+ *   index[L]    the concatenated 32-bit WAH words of all keys
+ * bit-exact with the reference's sequential `cpu` program
+ * (src/cpu.cpp:314-326).  Word format (src/cpu.cpp:201-211, :47-74): a literal
+ * has bit 31 set and bit (row % 31) for each row of its 31-row chunk; a fill
+ * has bit 31 clear and its low 30 bits count all-zero chunks.  Only zero
+ * fills are produced, never a trailing fill, and a full chunk stays a
+ * 0xFFFFFFFF literal.
+ *
+ * The reference drives the same path through CAF's OpenCL actor facade
+ * (caf::opencl::manager::spawn(program, kernel, nd_range, in/out tags...),
+ * src/phases.cpp:480-712, and the single-kernel variant src/gpu.cpp:356-367),
+ * moving data with dev->global_argument / mem_ref::data (src/phases.cpp:720,
+ * :1087-1088).  These entry points replace that facade: plain pointers and
+ * sizes, caller-owned device buffers, stream-ordered, never aborting.
+ *
+ * All device pointers must be 16-byte aligned (cudaMalloc gives 256).
+ * Functions return a WAH_* status; asynchronous device-side errors land in
+ * wah_counts.status and are valid after the stream is synchronised.
+ */
+#ifndef WAH_WAH_H
+#define WAH_WAH_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes.  The reference exits the process on any failure
+ * (valid_or_exit, src/phases.cpp:102-112); here every failure is a code. */
+#define WAH_OK 0
+#define WAH_EINVAL 1    /* null/misaligned pointer, bad size               */
+#define WAH_ENOMEM 2    /* workspace too small / allocation failed          */
+#define WAH_ECUDA 3     /* a CUDA runtime call failed                       */
+#define WAH_ETIMEOUT 4  /* a bounded device-side wait gave up               */
+#define WAH_ERANGE 5    /* n >= 2^30, or a value above the stated bound     */
+#define WAH_EOVERFLOW 6 /* an output would exceed the caller's capacity     */
+#define WAH_ENODEV 7    /* no usable sm_103 device                          */
+
+/* Largest column one call accepts (rows).  Offsets and index positions are
+ * u32 as in the reference; n < 2^30 keeps every counter in range. */
+#define WAH_MAX_ROWS ((uint64_t)1 << 30)
+
+/* Device-written result counters (16 bytes). */
+typedef struct wah_counts {
+  uint32_t keycnt;    /* K: distinct values (keycount, src/phases.cpp:1052)   */
+  uint32_t index_len; /* L: index words (index_length, src/phases.cpp:974)     */
+  uint32_t merged;    /* k: merged (value, chunk) entries (src/cpu.cpp:320)    */
+  uint32_t status;    /* WAH_OK or the first device-side error                 */
+} wah_counts;
+
+/* Human-readable name of a status code. */
+const char* wah_strerror(int status);
+
+/* Output capacities a caller must provide for a column of n rows whose
+ * values are all <= bound (bound == 0: unknown, any uint32).
+ * keys_cap = offsets_cap = min(n, bound + 1) (n when bound == 0);
+ * index_cap = 2n (L <= 2k <= 2n).  Replaces the reference's size lambdas
+ * (k_double, fills_k, ..., src/phases.cpp:405-438). */
+void wah_output_caps(uint64_t n, uint32_t bound, uint64_t* keys_cap,
+                     uint64_t* index_cap);
+
+/* Device workspace bytes wah_build needs for n rows.  Replaces the
+ * reference's scratch_argument buffers (src/phases.cpp:749-753). */
+size_t wah_workspace_bytes(uint64_t n, uint32_t bound);
+
+/*
+ * Builds the index of d_values[0..n) (device memory) on `stream`
+ * (a cudaStream_t; NULL = legacy default stream).  The whole of
+ * src/cpu.cpp:318-326 / src/phases.cpp:730-1077: sort_rids_by_value,
+ * produce_chunk_id_literals, merged_lit_by_val_chids, produce_fills,
+ * fuse_fill_literals, compute_colum_length.
+ *
+ * bound: largest value in the column, or 0 to let the device find out
+ * (the reference's -b/--bound flag, src/cpu.cpp:306-310).  With a bound the
+ * sort runs ceil(bits(bound)/8) digit passes; values above it are reported
+ * as WAH_ERANGE in d_counts->status.
+ * d_keys/d_offsets: capacity from wah_output_caps; d_index: 2n words.
+ * d_counts: device wah_counts, written at the end of the build.
+ * The call enqueues work and returns; nothing is synchronised.
+ * n == 0 writes K = L = 0 (the reference is undefined there).
+ */
+int wah_build(const uint32_t* d_values, uint64_t n, uint32_t bound,
+              uint32_t* d_keys, uint32_t* d_offsets, uint32_t* d_index,
+              wah_counts* d_counts, void* d_workspace, size_t workspace_bytes,
+              void* stream);
+
+/*
+ * Phase a1 alone: stable sort of d_values by value carrying row ids
+ * (src/cpu.cpp:180-197 semantics; src/phases.cpp:730-773 on the GPU).
+ * Writes d_sorted_values[n] and d_rids[n].  Same bound and workspace rules as
+ * wah_build.  d_status (optional, device u32) receives WAH_OK / error.
+ */
+int wah_sort_rids_by_value(const uint32_t* d_values, uint64_t n,
+                           uint32_t bound, uint32_t* d_sorted_values,
+                           uint32_t* d_rids, uint32_t* d_status,
+                           void* d_workspace, size_t workspace_bytes,
+                           void* stream);
+
+/*
+ * Phases a2-a6 fused, on an already sorted (value, rid) stream
+ * (src/cpu.cpp:319-326; src/phases.cpp:817-1077): chunk ids and literals,
+ * OR-merge per (value, chunk), fills, compaction into index, per-key counts
+ * and offsets.  Workspace: wah_workspace_bytes(n, bound) suffices.
+ */
+int wah_build_sorted(const uint32_t* d_sorted_values, const uint32_t* d_rids,
+                     uint64_t n, uint32_t* d_keys, uint32_t* d_offsets,
+                     uint32_t* d_index, wah_counts* d_counts,
+                     void* d_workspace, size_t workspace_bytes, void* stream);
+
+/*
+ * Host-buffer convenience path: the reference `phases` flow end to end
+ * (global_argument -> phases -> mem_ref::data, src/phases.cpp:720-1088).
+ * A context owns device buffers sized for columns up to max_n rows, a
+ * stream and a copy of the result counters.  Host buffers may be pageable or
+ * pinned (pinned is faster).  wah_ctx_build_host copies values in, builds,
+ * and copies keys[K], offsets[K], index[L] out; it returns when they are in
+ * host memory.  Host capacities as wah_output_caps.
+ */
+typedef struct wah_ctx wah_ctx;
+int wah_ctx_create(uint64_t max_n, uint32_t bound, wah_ctx** out);
+int wah_ctx_build_host(wah_ctx* ctx, const uint32_t* h_values, uint64_t n,
+                       uint32_t* h_keys, uint32_t* h_offsets, uint32_t* h_index,
+                       wah_counts* h_counts);
+void wah_ctx_destroy(wah_ctx* ctx);
+
+/* Number of kernels the last wah_build/wah_ctx_build_host on this thread
+ * enqueued (launch accounting for benchmarks). */
+uint32_t wah_last_launch_count(void);
+
+/*
+ * Per-phase device timing, the counterpart of the reference's
+ * SHOW_TIME_CONSUMPTION "N us" lines (src/phases.cpp:714-1127), measured with
+ * CUDA events on the build's own stream instead of host clocks around
+ * synchronisations.  wah_build_timed is wah_build plus event records around
+ * each kernel: events[2p] before and events[2p+1] after phase p, for the
+ * WAH_TIMED_PHASES phases histogram, plan, digit passes 0..3, index build
+ * (a pass that is not launched gets an empty span).  Events come from
+ * wah_events_create; durations from wah_events_elapsed after a sync.
+ */
+#define WAH_TIMED_PHASES 7
+int wah_events_create(uint32_t count, void** events);
+void wah_events_destroy(uint32_t count, void** events);
+int wah_events_elapsed(void* start, void* end, float* ms);
+int wah_build_timed(const uint32_t* d_values, uint64_t n, uint32_t bound,
+                    uint32_t* d_keys, uint32_t* d_offsets, uint32_t* d_index,
+                    wah_counts* d_counts, void* d_workspace,
+                    size_t workspace_bytes, void* stream, void** events);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* WAH_WAH_H */

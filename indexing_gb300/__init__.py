@@ -1,0 +1,271 @@
+"""GB300 WAH bitmap index builder.
+
+Python face of the C ABI in ``include/wah/wah.h`` (library
+``libwah_gb300.so``).  It mirrors the reference's phase interface
+(src/phases.cpp, src/cpu.cpp):
+
+* :func:`build_index`        whole pipeline (sort_rids_by_value ..
+                             compute_colum_length) on a device column
+* :func:`sort_rids_by_value` phase a1 alone
+* :func:`build_sorted`       phases a2..a6 on a sorted (value, rid) stream
+* :class:`HostContext`       host buffers in, host buffers out (the
+                             reference's global_argument -> phases ->
+                             mem_ref::data flow)
+* :func:`decoded_bitmap`     one key's words as a '0'/'1' string
+                             (src/cpu.cpp:47-74)
+
+Device memory comes from torch (plumbing only); every computation runs in
+the CUDA kernels of the native library.  There is no CPU fallback: without
+the library or a GPU these functions raise.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib
+from ._lib import wah_counts
+
+__all__ = ["WahError", "WahIndex", "build_index", "sort_rids_by_value", "build_sorted",
+           "HostContext", "decoded_bitmap", "workspace_bytes", "output_caps",
+           "MAX_ROWS", "last_launch_count"]
+
+MAX_ROWS = 1 << 30
+
+WAH_OK, WAH_EINVAL, WAH_ENOMEM, WAH_ECUDA, WAH_ETIMEOUT, WAH_ERANGE, WAH_EOVERFLOW, \
+    WAH_ENODEV = range(8)
+
+
+class WahError(RuntimeError):
+    """A non-zero status from the native library."""
+
+    def __init__(self, status: int, where: str = ""):
+        self.status = int(status)
+        msg = _lib.load().wah_strerror(self.status).decode()
+        super().__init__(f"{where}: {msg} (status {self.status})" if where else msg)
+
+
+def _check(rc: int, where: str) -> None:
+    if rc != WAH_OK:
+        raise WahError(rc, where)
+
+
+@dataclass
+class WahIndex:
+    """keys[K], offsets[K], index[L] plus the merged-entry count k."""
+    keys: object
+    offsets: object
+    index: object
+    merged: int
+
+    @property
+    def keycnt(self) -> int:
+        return len(self.keys)
+
+    @property
+    def index_len(self) -> int:
+        return len(self.index)
+
+    def bitmap(self, i: int):
+        """Words of the i-th key (src/cpu.cpp:332-335)."""
+        end = int(self.offsets[i + 1]) if i + 1 < len(self.offsets) else len(self.index)
+        return self.index[int(self.offsets[i]):end]
+
+    def numpy(self) -> "WahIndex":
+        def cv(a):
+            return a.cpu().numpy().view(np.uint32) if hasattr(a, "cpu") else a
+        return WahIndex(cv(self.keys), cv(self.offsets), cv(self.index), self.merged)
+
+
+def output_caps(n: int, bound: int = 0):
+    kc, ic = ctypes.c_uint64(), ctypes.c_uint64()
+    _lib.load().wah_output_caps(n, bound, ctypes.byref(kc), ctypes.byref(ic))
+    return kc.value, ic.value
+
+
+def workspace_bytes(n: int, bound: int = 0) -> int:
+    return int(_lib.load().wah_workspace_bytes(n, bound))
+
+
+def last_launch_count() -> int:
+    """Kernels enqueued by the last native call on this thread."""
+    return int(_lib.load().wah_last_launch_count())
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def _stream_handle(stream) -> int:
+    torch = _torch()
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return s.cuda_stream
+
+
+def _as_device_u32(values, device):
+    """uint32 data as a contiguous int32 CUDA tensor (same bits)."""
+    torch = _torch()
+    if isinstance(values, np.ndarray):
+        arr = np.ascontiguousarray(values, dtype=np.uint32).view(np.int32)
+        return torch.from_numpy(arr).to(device)
+    t = values
+    if t.dtype not in (torch.int32, torch.uint32):
+        raise TypeError("values must be a 32-bit integer tensor")
+    if t.dtype == torch.uint32:
+        t = t.view(torch.int32)
+    return t.to(device).contiguous()
+
+
+class _Buffers:
+    """Device outputs + workspace for one column (reusable)."""
+
+    def __init__(self, n: int, bound: int, device):
+        torch = _torch()
+        kc, ic = output_caps(max(n, 1), bound)
+        self.keys = torch.empty(kc, dtype=torch.int32, device=device)
+        self.offsets = torch.empty(kc, dtype=torch.int32, device=device)
+        self.index = torch.empty(ic, dtype=torch.int32, device=device)
+        self.counts = torch.zeros(4, dtype=torch.int32, device=device)
+        self.ws_bytes = workspace_bytes(max(n, 1), bound)
+        self.ws = torch.empty(self.ws_bytes, dtype=torch.uint8, device=device)
+
+
+def build_index(values, bound: int = 0, stream=None, device="cuda", sync: bool = True,
+                buffers: _Buffers | None = None) -> WahIndex:
+    """Builds the WAH index of one uint32 column on the GPU.
+
+    ``values``: numpy uint32 array or 32-bit integer tensor.  ``bound``: the
+    largest value (the reference's ``-b``), 0 = unknown.  Returns a
+    :class:`WahIndex` of CUDA int32 tensors holding uint32 bits (use
+    ``.numpy()`` for numpy uint32).  With ``sync=False`` the counters are not
+    read back and the full-capacity buffers are returned in a tuple instead.
+    """
+    lib = _lib.load()
+    torch = _torch()
+    v = _as_device_u32(values, device)
+    n = v.numel()
+    if n >= MAX_ROWS:
+        raise WahError(WAH_ERANGE, "build_index")
+    b = buffers or _Buffers(n, bound, v.device)
+    rc = lib.wah_build(v.data_ptr(), n, bound, b.keys.data_ptr(), b.offsets.data_ptr(),
+                       b.index.data_ptr(), b.counts.data_ptr(), b.ws.data_ptr(), b.ws_bytes,
+                       _stream_handle(stream))
+    _check(rc, "wah_build")
+    if not sync:
+        return b
+    c = b.counts.cpu().numpy().view(np.uint32)
+    if c[3] != WAH_OK:
+        raise WahError(int(c[3]), "wah_build (device)")
+    K, L, k = int(c[0]), int(c[1]), int(c[2])
+    return WahIndex(b.keys[:K], b.offsets[:K], b.index[:L], k)
+
+
+def sort_rids_by_value(values, bound: int = 0, stream=None, device="cuda"):
+    """Phase a1: (sorted values, rids) as CUDA int32 tensors (uint32 bits)."""
+    lib = _lib.load()
+    torch = _torch()
+    v = _as_device_u32(values, device)
+    n = v.numel()
+    out_v = torch.empty(max(n, 1), dtype=torch.int32, device=v.device)
+    out_r = torch.empty(max(n, 1), dtype=torch.int32, device=v.device)
+    status = torch.zeros(4, dtype=torch.int32, device=v.device)
+    wsb = workspace_bytes(max(n, 1), bound)
+    ws = torch.empty(wsb, dtype=torch.uint8, device=v.device)
+    rc = lib.wah_sort_rids_by_value(v.data_ptr(), n, bound, out_v.data_ptr(), out_r.data_ptr(),
+                                    status.data_ptr(), ws.data_ptr(), wsb,
+                                    _stream_handle(stream))
+    _check(rc, "wah_sort_rids_by_value")
+    st = int(status[0].item())
+    if st != WAH_OK:
+        raise WahError(st, "wah_sort_rids_by_value (device)")
+    return out_v[:n], out_r[:n]
+
+
+def build_sorted(sorted_values, rids, stream=None) -> WahIndex:
+    """Phases a2..a6 on an already sorted (value, rid) stream."""
+    lib = _lib.load()
+    torch = _torch()
+    sv = _as_device_u32(sorted_values, "cuda")
+    sr = _as_device_u32(rids, sv.device)
+    n = sv.numel()
+    b = _Buffers(n, 0, sv.device)
+    rc = lib.wah_build_sorted(sv.data_ptr(), sr.data_ptr(), n, b.keys.data_ptr(),
+                              b.offsets.data_ptr(), b.index.data_ptr(), b.counts.data_ptr(),
+                              b.ws.data_ptr(), b.ws_bytes, _stream_handle(stream))
+    _check(rc, "wah_build_sorted")
+    c = b.counts.cpu().numpy().view(np.uint32)
+    if c[3] != WAH_OK:
+        raise WahError(int(c[3]), "wah_build_sorted (device)")
+    K, L, k = int(c[0]), int(c[1]), int(c[2])
+    return WahIndex(b.keys[:K], b.offsets[:K], b.index[:L], k)
+
+
+class HostContext:
+    """Host buffers in, host buffers out, through ``wah_ctx_build_host``.
+
+    Device buffers for columns up to ``max_n`` rows are allocated once and
+    reused; each :meth:`build` copies the values in, builds, and copies keys,
+    offsets and index out (the reference ``phases`` flow,
+    src/phases.cpp:720-1088).
+    """
+
+    def __init__(self, max_n: int, bound: int = 0):
+        self._lib = _lib.load()
+        self.max_n = max_n
+        self.bound = bound
+        h = ctypes.c_void_p()
+        _check(self._lib.wah_ctx_create(max_n, bound, ctypes.byref(h)), "wah_ctx_create")
+        self._h = h
+        self.keys_cap, self.index_cap = output_caps(max(max_n, 1), bound)
+
+    def close(self):
+        if self._h:
+            self._lib.wah_ctx_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def build_into(self, values: np.ndarray, keys: np.ndarray, offsets: np.ndarray,
+                   index: np.ndarray) -> wah_counts:
+        """Build into caller-provided host arrays (pinned arrays are fastest)."""
+        v = np.ascontiguousarray(values, dtype=np.uint32)
+        cnt = wah_counts()
+        rc = self._lib.wah_ctx_build_host(self._h, v.ctypes.data, v.size, keys.ctypes.data,
+                                          offsets.ctypes.data, index.ctypes.data,
+                                          ctypes.byref(cnt))
+        _check(rc, "wah_ctx_build_host")
+        return cnt
+
+    def build(self, values: np.ndarray) -> WahIndex:
+        keys = np.empty(self.keys_cap, np.uint32)
+        offs = np.empty(self.keys_cap, np.uint32)
+        index = np.empty(self.index_cap, np.uint32)
+        c = self.build_into(values, keys, offs, index)
+        return WahIndex(keys[:c.keycnt], offs[:c.keycnt], index[:c.index_len], c.merged)
+
+
+def decoded_bitmap(words) -> str:
+    """One key's words decoded to a '0'/'1' string, trailing zeros trimmed
+    (src/cpu.cpp:47-74)."""
+    w = np.asarray(words.cpu().numpy() if hasattr(words, "cpu") else words).view(np.uint32)
+    parts = []
+    for block in w.tolist():
+        if block & 0x80000000:
+            parts.append("".join("1" if (block >> i) & 1 else "0" for i in range(31)))
+        else:
+            bit = "1" if block & 0x40000000 else "0"
+            parts.append(bit * (31 * (block & 0x3FFFFFFF)))
+    return "".join(parts).rstrip("0")

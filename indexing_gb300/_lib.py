@@ -1,0 +1,110 @@
+"""Loader and build recipe for the native library ``libwah_gb300.so``.
+
+The library holds the CUDA kernels and the C ABI declared in
+``include/wah/wah.h``.  It is built in-tree by ``nvcc`` for sm_103a only; the
+Python side never falls back to anything else: if the library is missing or
+cannot be loaded, importing the functions that need it raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from concurrent.futures import ThreadPoolExecutor
+
+PKG_DIR = os.path.dirname(os.path.abspath(__file__))
+REPO_DIR = os.path.dirname(PKG_DIR)
+CSRC = os.path.join(PKG_DIR, "csrc")
+INCLUDE = os.path.join(REPO_DIR, "include")
+OBJ_DIR = os.path.join(PKG_DIR, "_build")
+LIB_PATH = os.path.join(PKG_DIR, "libwah_gb300.so")
+
+CUDA_SOURCES = ["wah_sort.cu", "wah_index.cu", "wah_api.cu"]
+NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo",
+              "-std=c++17", "-Xcompiler", "-fPIC", "-I" + INCLUDE, "-I" + CSRC]
+
+
+def nvcc() -> str:
+    for cand in (os.environ.get("NVCC"), "/usr/local/cuda/bin/nvcc", "nvcc"):
+        if cand and (os.path.sep not in cand or os.path.exists(cand)):
+            return cand
+    return "nvcc"
+
+
+def build(verbose: bool = False) -> str:
+    """Compile every CUDA source (in parallel) and link libwah_gb300.so."""
+    os.makedirs(OBJ_DIR, exist_ok=True)
+    headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
+    headers.append(os.path.join(INCLUDE, "wah", "wah.h"))
+    newest_header = max(os.path.getmtime(h) for h in headers)
+
+    def compile_one(src: str) -> str:
+        obj = os.path.join(OBJ_DIR, src.replace(".cu", ".o"))
+        path = os.path.join(CSRC, src)
+        if (os.path.exists(obj) and os.path.getmtime(obj) >= os.path.getmtime(path)
+                and os.path.getmtime(obj) >= newest_header):
+            return obj
+        cmd = [nvcc(), *NVCC_FLAGS, "-c", path, "-o", obj]
+        if verbose:
+            cmd.insert(1, "-Xptxas=-v")
+        subprocess.run(cmd, check=True)
+        return obj
+
+    with ThreadPoolExecutor(max_workers=len(CUDA_SOURCES)) as ex:
+        objs = list(ex.map(compile_one, CUDA_SOURCES))
+    if (not os.path.exists(LIB_PATH)
+            or any(os.path.getmtime(o) > os.path.getmtime(LIB_PATH) for o in objs)):
+        subprocess.run([nvcc(), "-gencode", "arch=compute_103a,code=sm_103a", "-shared",
+                        *objs, "-o", LIB_PATH], check=True)
+    return LIB_PATH
+
+
+class wah_counts(ctypes.Structure):
+    _fields_ = [("keycnt", ctypes.c_uint32), ("index_len", ctypes.c_uint32),
+                ("merged", ctypes.c_uint32), ("status", ctypes.c_uint32)]
+
+
+# Exported symbols and their signatures (must match include/wah/wah.h).
+_vp = ctypes.c_void_p
+_u64 = ctypes.c_uint64
+_u32 = ctypes.c_uint32
+SIGNATURES = {
+    "wah_strerror": ([ctypes.c_int], ctypes.c_char_p),
+    "wah_output_caps": ([_u64, _u32, ctypes.POINTER(_u64), ctypes.POINTER(_u64)], None),
+    "wah_workspace_bytes": ([_u64, _u32], ctypes.c_size_t),
+    "wah_build": ([_vp, _u64, _u32, _vp, _vp, _vp, _vp, _vp, ctypes.c_size_t, _vp],
+                  ctypes.c_int),
+    "wah_sort_rids_by_value": ([_vp, _u64, _u32, _vp, _vp, _vp, _vp, ctypes.c_size_t, _vp],
+                               ctypes.c_int),
+    "wah_build_sorted": ([_vp, _vp, _u64, _vp, _vp, _vp, _vp, _vp, ctypes.c_size_t, _vp],
+                         ctypes.c_int),
+    "wah_ctx_create": ([_u64, _u32, ctypes.POINTER(_vp)], ctypes.c_int),
+    "wah_ctx_build_host": ([_vp, _vp, _u64, _vp, _vp, _vp, ctypes.POINTER(wah_counts)],
+                           ctypes.c_int),
+    "wah_ctx_destroy": ([_vp], None),
+    "wah_last_launch_count": ([], _u32),
+    "wah_events_create": ([_u32, ctypes.POINTER(_vp)], ctypes.c_int),
+    "wah_events_destroy": ([_u32, ctypes.POINTER(_vp)], None),
+    "wah_events_elapsed": ([_vp, _vp, ctypes.POINTER(ctypes.c_float)], ctypes.c_int),
+    "wah_build_timed": ([_vp, _u64, _u32, _vp, _vp, _vp, _vp, _vp, ctypes.c_size_t, _vp,
+                         ctypes.POINTER(_vp)], ctypes.c_int),
+}
+
+_lib = None
+
+
+def load() -> ctypes.CDLL:
+    """Load libwah_gb300.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(
+                f"{LIB_PATH} is missing: build it with "
+                "`python -c 'import __graft_entry__ as g; g.build()'`")
+        lib = ctypes.CDLL(LIB_PATH)
+        for name, (args, res) in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.argtypes = args
+            fn.restype = res
+        _lib = lib
+    return _lib

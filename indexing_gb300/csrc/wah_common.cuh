@@ -1,0 +1,224 @@
+// wah_common.cuh -- shared device helpers for the GB300 WAH index kernels.
+//
+// Layout of one build's device state (all in the caller's workspace):
+//   WahCtrl            digit histograms, per-pass bin offsets, pass plan,
+//                      dynamic tile counters
+//   sort look-back     one u32 per (tile, bin) for the onesweep passes
+//   build look-back    one u64 per tile for the fused index build
+//   ping-pong buffers  sorted keys and row ids, 4 x n u32
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "wah/wah.h"
+
+namespace wah {
+
+constexpr int kRadixBits = 8;
+constexpr int kRadix = 1 << kRadixBits;  // 256 bins per digit
+constexpr int kDigits = 4;               // 32-bit keys -> up to 4 passes
+
+// Onesweep pass: 256 threads (one per bin in the look-back), 16 keys each.
+constexpr int kSortThreads = 256;
+constexpr int kSortItems = 16;
+constexpr int kSortTile = kSortThreads * kSortItems;  // 4096 rows
+
+// Fused index build: 256 threads x 8 rows, blocked.
+constexpr int kBuildThreads = 256;
+constexpr int kBuildItems = 8;
+constexpr int kBuildTile = kBuildThreads * kBuildItems;  // 2048 rows
+
+constexpr int kHistThreads = 256;
+constexpr int kHistUnroll = 4;  // uint4 loads in flight per thread
+
+// Look-back status in the top two bits of an entry.
+constexpr uint32_t kLbFlagShift32 = 30;
+constexpr uint32_t kLbAggregate32 = 1u << 30;
+constexpr uint32_t kLbPrefix32 = 2u << 30;
+constexpr uint32_t kLbMask32 = (1u << 30) - 1;
+constexpr uint64_t kLbAggregate64 = 1ull << 62;
+constexpr uint64_t kLbPrefix64 = 2ull << 62;
+constexpr uint64_t kLbMask64 = (1ull << 62) - 1;
+
+// Bounded waits: after kSpinFast polls a waiter sleeps between polls; after
+// kSpinLimit polls it gives up, records WAH_ETIMEOUT and carries on without
+// writing anything it could not place.
+constexpr uint32_t kSpinFast = 64;
+constexpr uint32_t kSpinLimit = 1u << 22;
+
+// Source/destination selectors of a sort pass.
+constexpr int kSelInput = 0;  // the caller's values, rid = row index
+constexpr int kSelA = 1;
+constexpr int kSelB = 2;
+
+struct WahCtrl {
+  uint32_t hist[kDigits][kRadix];     // rows per digit value, per pass
+  uint32_t bin_off[kDigits][kRadix];  // exclusive scan of hist
+  int32_t pass_src[kDigits];          // -1: pass skipped (trivial digit)
+  int32_t pass_dst[kDigits];
+  int32_t final_sel;                  // where the sorted stream ends up
+  uint32_t tile_ctr[8];               // [0..3] sort passes, [4] build
+  uint32_t pad[3];
+};
+
+// Pointers of the three possible key/rid homes (input, A, B).
+struct SortBufs {
+  const uint32_t* keys[3];
+  const uint32_t* rids[3];  // rids[kSelInput] == nullptr: rid = row index
+};
+
+__host__ __device__ constexpr inline uint64_t ceil_div(uint64_t a, uint64_t b) {
+  return (a + b - 1) / b;
+}
+
+#if defined(__CUDACC__)
+
+__device__ __forceinline__ uint32_t ld_relaxed_u32(const uint32_t* p) {
+  uint32_t v;
+  asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_relaxed_u32(uint32_t* p, uint32_t v) {
+  asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ uint64_t ld_relaxed_u64(const uint64_t* p) {
+  uint64_t v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_relaxed_u64(uint64_t* p, uint64_t v) {
+  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+// Streaming 128-bit load (read once: do not keep in L1).
+__device__ __forceinline__ uint4 ld_stream_v4(const uint4* p) {
+  uint4 v;
+  asm volatile("ld.global.cs.v4.u32 {%0,%1,%2,%3}, [%4];"
+               : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+               : "l"(p));
+  return v;
+}
+
+__device__ __forceinline__ uint32_t lanemask_lt() {
+  uint32_t m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+// First error wins.
+__device__ __forceinline__ void set_status(uint32_t* status, uint32_t code) {
+  if (status) atomicCAS(status, 0u, code);
+}
+
+// Exclusive scan of one u32 per thread across a block of THREADS threads.
+// Returns the thread's exclusive prefix; *total gets the block sum.
+template <int THREADS>
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t x, uint32_t* total,
+                                                         uint32_t* s_warp /* >= THREADS/32 */) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t incl = x;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    uint32_t y = __shfl_up_sync(0xffffffffu, incl, d);
+    if (lane >= d) incl += y;
+  }
+  if (lane == 31) s_warp[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t w = lane < THREADS / 32 ? s_warp[lane] : 0;
+    uint32_t wi = w;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      uint32_t y = __shfl_up_sync(0xffffffffu, wi, d);
+      if (lane >= d) wi += y;
+    }
+    if (lane < THREADS / 32) s_warp[lane] = wi - w;  // exclusive warp prefix
+    if (lane == THREADS / 32 - 1) s_warp[THREADS / 32] = wi;
+  }
+  __syncthreads();
+  uint32_t r = s_warp[warp] + incl - x;
+  *total = s_warp[THREADS / 32];
+  __syncthreads();  // s_warp reusable after return
+  return r;
+}
+
+// Same for 64-bit packed counters (no carries between fields by construction).
+template <int THREADS>
+__device__ __forceinline__ uint64_t block_exclusive_scan64(uint64_t x, uint64_t* total,
+                                                           uint64_t* s_warp) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint64_t incl = x;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    uint64_t y = __shfl_up_sync(0xffffffffu, incl, d);
+    if (lane >= d) incl += y;
+  }
+  if (lane == 31) s_warp[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    uint64_t w = lane < THREADS / 32 ? s_warp[lane] : 0;
+    uint64_t wi = w;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      uint64_t y = __shfl_up_sync(0xffffffffu, wi, d);
+      if (lane >= d) wi += y;
+    }
+    if (lane < THREADS / 32) s_warp[lane] = wi - w;
+    if (lane == THREADS / 32 - 1) s_warp[THREADS / 32] = wi;
+  }
+  __syncthreads();
+  uint64_t r = s_warp[warp] + incl - x;
+  *total = s_warp[THREADS / 32];
+  __syncthreads();
+  return r;
+}
+
+#endif  // __CUDACC__
+
+// Timed phases (wah_build_timed): histogram, plan, four digit passes, build.
+constexpr int kPhaseHist = 0;
+constexpr int kPhasePlan = 1;
+constexpr int kPhasePass0 = 2;
+constexpr int kPhaseBuild = 6;
+constexpr int kPhases = 7;
+
+inline void record_phase(cudaEvent_t* ev, int phase, bool end, cudaStream_t s) {
+  if (ev) cudaEventRecord(ev[2 * phase + (end ? 1 : 0)], s);
+}
+
+// Host-side launchers (defined in the .cu files).
+struct SortLaunch {
+  const uint32_t* values;
+  uint64_t n;
+  int passes;  // digit passes to launch (1..4)
+  WahCtrl* ctrl;
+  uint32_t* lb_sort;  // tiles * 256 u32
+  uint32_t* buf_keys[2];
+  uint32_t* buf_rids[2];
+  uint32_t* status;
+  int sm_count;
+  cudaEvent_t* events;  // optional: [2*phase] before, [2*phase+1] after
+};
+cudaError_t launch_sort(const SortLaunch& a, cudaStream_t s, uint32_t* launches);
+cudaError_t launch_sort_deliver(const SortBufs& bufs, const WahCtrl* ctrl, uint64_t n,
+                                uint32_t* out_keys, uint32_t* out_rids, cudaStream_t s,
+                                uint32_t* launches);
+
+struct BuildLaunch {
+  SortBufs src;
+  int sel;  // -1: take WahCtrl::final_sel, else a fixed selector
+  uint64_t n;
+  WahCtrl* ctrl;
+  uint64_t* lb_build;  // tiles u64
+  uint32_t* keys;
+  uint32_t* offsets;
+  uint32_t* index;
+  uint64_t keys_cap;
+  uint64_t index_cap;
+  wah_counts* counts;
+  cudaEvent_t* events;  // optional, phase kPhaseBuild
+};
+cudaError_t launch_build(const BuildLaunch& a, cudaStream_t s, uint32_t* launches);
+
+}  // namespace wah

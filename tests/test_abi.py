@@ -1,0 +1,62 @@
+"""The C-ABI library loads and exports every symbol include/wah/wah.h
+declares; host-only entry points behave without a GPU."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from indexing_gb300 import _lib
+
+HEADER = os.path.join(_lib.INCLUDE, "wah", "wah.h")
+
+
+def declared_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    names = re.findall(r"^[A-Za-z_][\w\s\*]*?\b(wah_\w+)\s*\(", text, flags=re.M)
+    return sorted(set(names))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    if not os.path.exists(_lib.LIB_PATH):
+        _lib.build()
+    return _lib.load()
+
+
+def test_header_declares_the_boundary():
+    names = declared_functions()
+    for must in ("wah_build", "wah_workspace_bytes", "wah_strerror", "wah_sort_rids_by_value",
+                 "wah_build_sorted", "wah_ctx_create", "wah_ctx_build_host",
+                 "wah_ctx_destroy", "wah_output_caps"):
+        assert must in names
+
+
+def test_every_declared_symbol_is_exported(lib):
+    for name in declared_functions():
+        assert hasattr(lib, name), name
+        assert name in _lib.SIGNATURES, f"{name} has no ctypes signature"
+
+
+def test_strerror(lib):
+    assert lib.wah_strerror(0) == b"ok"
+    assert b"range" in lib.wah_strerror(5)
+    assert lib.wah_strerror(999) == b"unknown status"
+
+
+def test_output_caps_and_workspace(lib):
+    kc, ic = ctypes.c_uint64(), ctypes.c_uint64()
+    lib.wah_output_caps(1000, 0, ctypes.byref(kc), ctypes.byref(ic))
+    assert (kc.value, ic.value) == (1000, 2000)
+    lib.wah_output_caps(1 << 20, 65535, ctypes.byref(kc), ctypes.byref(ic))
+    assert (kc.value, ic.value) == (65536, 1 << 21)
+    ws = lib.wah_workspace_bytes(1 << 20, 0)
+    assert ws >= 16 * (1 << 20)  # four ping-pong columns
+    assert lib.wah_workspace_bytes(1 << 20, 0) < lib.wah_workspace_bytes(1 << 21, 0)
+
+
+def test_rejects_oversize_without_touching_device(lib):
+    # n >= 2^30 is refused before any CUDA call
+    rc = lib.wah_build(None, 1 << 30, 0, None, None, None, ctypes.c_void_p(16), None, 0, None)
+    assert rc == 5

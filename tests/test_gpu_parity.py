@@ -1,0 +1,127 @@
+"""Parity of the CUDA path (through the C ABI) with the oracle and with the
+golden vectors made by the reference's own code.  Integer work: bit-exact."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+@pytest.fixture(scope="module")
+def wah():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import indexing_gb300 as w
+    w._lib.load()
+    return w
+
+
+def assert_same(gpu_idx, ref, name=""):
+    g = gpu_idx.numpy()
+    assert np.array_equal(g.keys, ref.keys), f"{name}: keys differ"
+    assert np.array_equal(g.offsets, ref.offsets), f"{name}: offsets differ"
+    assert g.index.size == ref.index.size, f"{name}: L {g.index.size} != {ref.index.size}"
+    assert np.array_equal(g.index, ref.index), f"{name}: index words differ"
+    assert g.merged == ref.merged, f"{name}: k {g.merged} != {ref.merged}"
+
+
+def test_golden_vectors(wah, golden):
+    for name, case in golden.items():
+        ref = O.Index(case["keys"], case["offsets"], case["index"], int(case["merged"][0]))
+        assert_same(wah.build_index(case["values"]), ref, name)
+        # with the exact bound as the -b flag
+        bound = int(case["values"].max())
+        assert_same(wah.build_index(case["values"], bound=bound), ref, name + "/bound")
+
+
+def gen(kind, n, rng):
+    if kind == "uniform16":
+        return rng.integers(0, 65536, size=n, dtype=np.uint32)
+    if kind == "few16":
+        return rng.integers(0, 16, size=n, dtype=np.uint32)
+    if kind == "u32":
+        return rng.integers(0, 2 ** 32, size=n, dtype=np.uint64).astype(np.uint32)
+    if kind == "zipf":
+        w = 1.0 / np.arange(1, 65537, dtype=np.float64) ** 1.1
+        cdf = np.cumsum(w) / w.sum()
+        return np.minimum(np.searchsorted(cdf, rng.random(n)), 65535).astype(np.uint32)
+    if kind == "runs":
+        runs = rng.geometric(1 / 1000, size=n // 500 + 2)
+        vals = rng.integers(0, 65536, size=runs.size, dtype=np.uint32)
+        return np.repeat(vals, runs)[:n]
+    if kind == "const":
+        return np.full(n, 77, np.uint32)
+    if kind == "two":
+        return rng.integers(0, 2, size=n, dtype=np.uint32)
+    raise ValueError(kind)
+
+
+@pytest.mark.parametrize("kind", ["uniform16", "few16", "u32", "zipf", "runs", "const", "two"])
+@pytest.mark.parametrize("n", [1, 30, 31, 33, 1000, 2048, 4096, 4097, 100_003, 1 << 20])
+def test_random_columns(wah, kind, n):
+    rng = np.random.default_rng(hash((kind, n)) & 0xFFFFFFFF)
+    v = gen(kind, n, rng)
+    assert_same(wah.build_index(v), O.build(v), f"{kind}/{n}")
+
+
+def test_config1_uniform_1m_with_bound(wah):
+    # 1,048,576 uniform [0, 65535], seeded; bound given as the reference's -b
+    rng = np.random.default_rng(1)
+    v = rng.integers(0, 65536, size=1 << 20, dtype=np.uint32)
+    ref = O.build(v)
+    assert_same(wah.build_index(v, bound=65535), ref, "c1")
+    assert_same(wah.build_index(v, bound=0), ref, "c1/scan")
+
+
+def test_sort_phase_matches_stable_sort(wah):
+    rng = np.random.default_rng(3)
+    for n, m in ((1, 5), (5000, 7), (300_000, 65536), (70_001, 2 ** 32)):
+        v = rng.integers(0, m, size=n, dtype=np.uint64).astype(np.uint32)
+        sv, sr = wah.sort_rids_by_value(v)
+        ev, er = O.sort_rids_by_value(v)
+        assert np.array_equal(sv.cpu().numpy().view(np.uint32), ev)
+        assert np.array_equal(sr.cpu().numpy().view(np.uint32), er)
+
+
+def test_build_sorted_phase(wah):
+    rng = np.random.default_rng(4)
+    v = rng.integers(0, 1000, size=123_457, dtype=np.uint32)
+    ev, er = O.sort_rids_by_value(v)
+    assert_same(wah.build_sorted(ev, er), O.build(v), "build_sorted")
+
+
+def test_host_context_roundtrip(wah):
+    rng = np.random.default_rng(6)
+    with wah.HostContext(1 << 18) as ctx:
+        for n in (0, 1, 999, 1 << 18):
+            v = rng.integers(0, 5000, size=n, dtype=np.uint32)
+            got = ctx.build(v)
+            ref = O.build(v)
+            assert np.array_equal(got.keys, ref.keys)
+            assert np.array_equal(got.offsets, ref.offsets)
+            assert np.array_equal(got.index, ref.index)
+
+
+def test_empty_column(wah):
+    r = wah.build_index(np.zeros(0, np.uint32))
+    assert r.keycnt == 0 and r.index_len == 0
+
+
+def test_value_above_bound_is_reported(wah):
+    v = np.array([1, 2, 70000, 3], np.uint32)  # needs 3 digits, bound says 1
+    with pytest.raises(wah.WahError) as e:
+        wah.build_index(v, bound=255)
+    assert e.value.status == wah.WAH_ERANGE
+
+
+def test_decoded_bitmaps_match_rows(wah):
+    rng = np.random.default_rng(8)
+    v = gen("runs", 50_000, rng)
+    idx = wah.build_index(v).numpy()
+    for i in range(0, idx.keycnt, max(1, idx.keycnt // 20)):
+        rows = np.flatnonzero(v == idx.keys[i])
+        s = wah.decoded_bitmap(idx.bitmap(i))
+        assert [j for j, ch in enumerate(s) if ch == "1"] == rows.tolist()
