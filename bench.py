@@ -56,6 +56,8 @@ def parse():
     ap.add_argument("--seed", type=int, default=20170101)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--sort-items", type=int, default=0,
+                    help="onesweep rows per thread (0: library default)")
     ap.add_argument("--cpu-sample", type=int, default=1 << 23,
                     help="rows per oracle build in the CPU legs")
     return ap.parse_args()
@@ -205,6 +207,9 @@ def main():
         dist.init_process_group("nccl", device_id=dev)
 
     lib = _lib.load()
+    if args.sort_items:
+        if lib.wah_set_tuning(args.sort_items) != 0:
+            raise SystemExit(f"unsupported --sort-items {args.sort_items}")
     n, card = args.n, args.card
     bound = card - 1
     values_np = gen_uniform(n, card, args.seed + rank)
@@ -357,6 +362,7 @@ def main():
                        "rows": n, "bound": bound, "parallelism": f"replicas x{world}",
                        "l2": "inputs larger than L2 (1 GiB column), no flush"},
             "outputs": {"keycnt": K, "index_len": L, "merged": k},
+            "sort_items": int(lib.wah_get_tuning()),
             "hbm_gbs_pipeline": total_alg / (ms_per_step / 1e3) / 1e9,
             "phase_us": {p: round(phase_ms[p] * 1e3, 1) for p in PHASES},
             "roofline": {"bound": "hbm", "kernel": dom, "per_unit": per_unit.get(dom),

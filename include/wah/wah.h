@@ -135,6 +135,13 @@ void wah_ctx_destroy(wah_ctx* ctx);
  * enqueued (launch accounting for benchmarks). */
 uint32_t wah_last_launch_count(void);
 
+/* Tile shape of the onesweep digit passes: rows per thread (8, 12, 16 or 20;
+ * 256 threads per tile).  Process-wide; set by the autotuner or the caller
+ * before builds are enqueued.  The reference hard-codes its radix shape
+ * (src/phases.cpp:445-453). */
+int wah_set_tuning(int sort_items);
+int wah_get_tuning(void);
+
 /*
  * Per-phase device timing, the counterpart of the reference's
  * SHOW_TIME_CONSUMPTION "N us" lines (src/phases.cpp:714-1127), measured with

@@ -83,6 +83,8 @@ SIGNATURES = {
                            ctypes.c_int),
     "wah_ctx_destroy": ([_vp], None),
     "wah_last_launch_count": ([], _u32),
+    "wah_set_tuning": ([ctypes.c_int], ctypes.c_int),
+    "wah_get_tuning": ([], ctypes.c_int),
     "wah_events_create": ([_u32, ctypes.POINTER(_vp)], ctypes.c_int),
     "wah_events_destroy": ([_u32, ctypes.POINTER(_vp)], None),
     "wah_events_elapsed": ([_vp, _vp, ctypes.POINTER(ctypes.c_float)], ctypes.c_int),

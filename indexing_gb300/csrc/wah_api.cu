@@ -14,6 +14,7 @@ namespace wah {
 namespace {
 
 thread_local uint32_t g_last_launches = 0;
+int g_sort_items = 16;  // onesweep rows per thread (wah_set_tuning)
 
 constexpr size_t kAlign = 256;
 inline size_t align_up(size_t x) { return (x + kAlign - 1) / kAlign * kAlign; }
@@ -28,7 +29,8 @@ WsLayout ws_layout(uint64_t n) {
   l.ctrl = off;
   off += align_up(sizeof(WahCtrl));
   l.lb_sort = off;
-  off += align_up(ceil_div(std::max<uint64_t>(n, 1), kSortTile) * kRadix * sizeof(uint32_t));
+  off += align_up(ceil_div(std::max<uint64_t>(n, 1), (uint64_t)kSortThreads * kSortMinItems) *
+                  kRadix * sizeof(uint32_t));
   l.lb_build = off;
   off += align_up(ceil_div(std::max<uint64_t>(n, 1), kBuildTile) * sizeof(uint64_t));
   const size_t col = align_up(std::max<uint64_t>(n, 1) * sizeof(uint32_t));
@@ -92,6 +94,7 @@ int enqueue_sort(const uint32_t* d_values, uint64_t n, uint32_t bound, const WsL
   a.buf_rids[1] = reinterpret_cast<uint32_t*>(ws + l.rids_b);
   a.status = status;
   a.events = events;
+  a.sort_items = g_sort_items;
   a.sm_count = sm_count_current();
   if (a.sm_count <= 0) return WAH_ENODEV;
   e = launch_sort(a, s, launches);
@@ -136,6 +139,15 @@ void wah_output_caps(uint64_t n, uint32_t bound, uint64_t* keys_cap, uint64_t* i
 size_t wah_workspace_bytes(uint64_t n, uint32_t /*bound*/) { return ws_layout(n).total; }
 
 uint32_t wah_last_launch_count(void) { return g_last_launches; }
+
+int wah_set_tuning(int sort_items) {
+  if (sort_items != 8 && sort_items != 12 && sort_items != 16 && sort_items != 20)
+    return WAH_EINVAL;
+  g_sort_items = sort_items;
+  return WAH_OK;
+}
+
+int wah_get_tuning(void) { return g_sort_items; }
 
 static int build_impl(const uint32_t* d_values, uint64_t n, uint32_t bound, uint32_t* d_keys,
                       uint32_t* d_offsets, uint32_t* d_index, wah_counts* d_counts,
@@ -251,6 +263,7 @@ int wah_build_sorted(const uint32_t* d_sorted_values, const uint32_t* d_rids, ui
   if (n == 0) return WAH_OK;
   if (!d_sorted_values || !d_rids || !d_keys || !d_offsets || !d_index || !d_workspace)
     return WAH_EINVAL;
+  if (!aligned16(d_sorted_values) || !aligned16(d_rids)) return WAH_EINVAL;
   const WsLayout l = ws_layout(n);
   if (workspace_bytes < l.total) return WAH_ENOMEM;
   unsigned char* ws = static_cast<unsigned char*>(d_workspace);

@@ -19,10 +19,10 @@ constexpr int kRadixBits = 8;
 constexpr int kRadix = 1 << kRadixBits;  // 256 bins per digit
 constexpr int kDigits = 4;               // 32-bit keys -> up to 4 passes
 
-// Onesweep pass: 256 threads (one per bin in the look-back), 16 keys each.
+// Onesweep pass: 256 threads (one per bin in the look-back); rows per thread
+// is a tuning choice (8/12/16/20), kSortMinItems bounds the look-back array.
 constexpr int kSortThreads = 256;
-constexpr int kSortItems = 16;
-constexpr int kSortTile = kSortThreads * kSortItems;  // 4096 rows
+constexpr int kSortMinItems = 8;
 
 // Fused index build: 256 threads x 8 rows, blocked.
 constexpr int kBuildThreads = 256;
@@ -31,6 +31,7 @@ constexpr int kBuildTile = kBuildThreads * kBuildItems;  // 2048 rows
 
 constexpr int kHistThreads = 256;
 constexpr int kHistUnroll = 4;  // uint4 loads in flight per thread
+constexpr int kHistWarps = kHistThreads / 32;
 
 // Look-back status in the top two bits of an entry.
 constexpr uint32_t kLbFlagShift32 = 30;
@@ -59,7 +60,8 @@ struct WahCtrl {
   int32_t pass_dst[kDigits];
   int32_t final_sel;                  // where the sorted stream ends up
   uint32_t tile_ctr[8];               // [0..3] sort passes, [4] build
-  uint32_t pad[3];
+  uint32_t key_or;                    // OR of all keys (range check vs bound)
+  uint32_t pad[2];
 };
 
 // Pointers of the three possible key/rid homes (input, A, B).
@@ -104,6 +106,17 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
   uint32_t m;
   asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
   return m;
+}
+__device__ __forceinline__ uint32_t lanemask_gt() {
+  uint32_t m;
+  asm("mov.u32 %0, %%lanemask_gt;" : "=r"(m));
+  return m;
+}
+// Bit-field extract of `len` bits starting at `pos`.
+__device__ __forceinline__ uint32_t bfe(uint32_t x, uint32_t pos, uint32_t len) {
+  uint32_t r;
+  asm("bfe.u32 %0, %1, %2, %3;" : "=r"(r) : "r"(x), "r"(pos), "r"(len));
+  return r;
 }
 
 // First error wins.
@@ -198,8 +211,10 @@ struct SortLaunch {
   uint32_t* buf_rids[2];
   uint32_t* status;
   int sm_count;
+  int sort_items;       // onesweep rows per thread (8, 12, 16, 20)
   cudaEvent_t* events;  // optional: [2*phase] before, [2*phase+1] after
 };
+uint64_t sort_tiles(uint64_t n, int items);
 cudaError_t launch_sort(const SortLaunch& a, cudaStream_t s, uint32_t* launches);
 cudaError_t launch_sort_deliver(const SortBufs& bufs, const WahCtrl* ctrl, uint64_t n,
                                 uint32_t* out_keys, uint32_t* out_rids, cudaStream_t s,

@@ -14,34 +14,47 @@
 // The reference GPU path runs these as ~20 kernels with three stream
 // compactions and host read-backs of k (src/phases.cpp:817-1077).
 //
-// Here one kernel does all of it.  A tile of 2048 sorted rows sits in shared
-// memory with one row of look-behind (to classify the first row) and 30 rows
-// of look-ahead (a (value, chunk) segment has at most 31 rows, so the tile
-// that owns a segment's head can finish its literal).  Each row is classified
+// Here one kernel does all of it, over tiles of 2048 sorted rows (256
+// threads x 8 consecutive rows, loaded with 128-bit loads into registers and
+// mirrored in shared memory with one row of look-behind and 30 rows of
+// look-ahead: a (value, chunk) segment has at most 31 rows, so the tile that
+// owns a segment's head can finish its literal).  Each row is classified
 // locally: segment head when (value, chunk) changes, value head when the
-// value changes; a head emits 1 + (fill != 0) words.  A block scan plus a
+// value changes; a head emits 1 + (fill != 0) words.  Literals come from a
+// reverse segmented OR over the thread's rows.  One packed block scan plus a
 // decoupled look-back across tiles (64-bit entries carrying the word and key
-// prefixes together) gives every head its final position, so the words are
-// written once, in place, with no zero words and no compaction pass.  Keys
-// and offsets fall out of the same scan at value heads.
+// prefixes together) gives every head its final position; words, keys and
+// offsets are staged in shared memory and written once, coalesced, with no
+// zero words and no compaction pass.
 #include "wah_common.cuh"
 
 namespace wah {
 
-__device__ __forceinline__ uint32_t pad_idx(uint32_t i) { return i + (i >> 5); }
+constexpr int kLookAhead = 30;  // a segment has at most 31 rows
+constexpr int kWinRows = kBuildTile + kLookAhead + 2;
 
-constexpr int kWindow = kBuildTile + 31;  // 1 behind + tile + 30 ahead
-constexpr int kWindowPadded = kWindow + kWindow / 32 + 1;
+// Staging index skew: position i lives at i + i/16, so threads writing runs
+// that start ~16 words apart hit different banks.
+__device__ __forceinline__ uint32_t skew(uint32_t i) { return i + (i >> 4); }
+constexpr int kSkewed(int n) { return n + n / 16 + 1; }
 
 struct BuildSmem {
-  uint32_t v[kWindowPadded];
-  uint32_t r[kWindowPadded];
-  uint32_t words[2 * kBuildTile];  // staged index words of this tile
+  uint32_t v[kWinRows];   // sorted values of rows base .. base+TILE+29
+  uint32_t cb[kWinRows];  // (chunk << 5) | (rid % 31) of the same rows
+  uint32_t words[kSkewed(2 * kBuildTile)];
+  uint32_t keys[kSkewed(kBuildTile)];
+  uint32_t offs[kSkewed(kBuildTile)];
   uint64_t warp_tmp[kBuildThreads / 32 + 1];
-  uint64_t tile_prefix;            // exclusive (keys << 32 | words) prefix
+  uint64_t tile_prefix;  // exclusive (keys << 32 | words) before this tile
+  uint32_t prev_v, prev_cb;
   uint32_t tile;
   int abort;
 };
+
+__device__ __forceinline__ uint32_t chunk_bit(uint32_t rid) {
+  const uint32_t c = rid / 31;
+  return (c << 5) | (rid - c * 31);
+}
 
 // Look-back over earlier tiles by warp 0; returns the exclusive prefix.
 __device__ __forceinline__ uint64_t build_lookback(uint64_t* __restrict__ lb, uint32_t tile,
@@ -76,6 +89,10 @@ __device__ __forceinline__ uint64_t build_lookback(uint64_t* __restrict__ lb, ui
   return excl;
 }
 
+// Per-thread counters packed for one block scan: words | keys << 21 | segs << 42.
+constexpr int kPackShift = 21;
+constexpr uint64_t kPackMask = (1ull << kPackShift) - 1;
+
 __global__ void __launch_bounds__(kBuildThreads, 4)
     k_wah_build(SortBufs bufs, int sel, uint64_t n, WahCtrl* ctrl, uint64_t* __restrict__ lb,
                 uint32_t* __restrict__ keys, uint32_t* __restrict__ offsets,
@@ -86,10 +103,10 @@ __global__ void __launch_bounds__(kBuildThreads, 4)
   uint32_t* status = &counts->status;
 
   const int s = sel >= 0 ? sel : ctrl->final_sel;
-  const uint32_t* __restrict__ sv = bufs.keys[s];
-  const uint32_t* __restrict__ sr = bufs.rids[s];  // null: rid = row index
+  const uint32_t* __restrict__ sv = s == 0 ? bufs.keys[0] : (s == 1 ? bufs.keys[1] : bufs.keys[2]);
+  const uint32_t* __restrict__ sr = s == 0 ? bufs.rids[0] : (s == 1 ? bufs.rids[1] : bufs.rids[2]);
 
-  const int tid = threadIdx.x;
+  const uint32_t tid = threadIdx.x;
   if (tid == 0) {
     sm.tile = atomicAdd(&ctrl->tile_ctr[4], 1u);
     sm.abort = 0;
@@ -97,136 +114,175 @@ __global__ void __launch_bounds__(kBuildThreads, 4)
   __syncthreads();
   const uint32_t tile = sm.tile;
   const uint64_t base = (uint64_t)tile * kBuildTile;
+  const bool full = base + kBuildTile <= n;
+  const uint32_t valid = full ? kBuildTile : (uint32_t)(n - base);
+  // rows of the window that exist (tile + look-ahead, clipped at n)
+  const uint64_t left = n - base;
+  const uint32_t wend = left < (uint64_t)(kBuildTile + kLookAhead) ? (uint32_t)left
+                                                                    : (uint32_t)(kBuildTile + kLookAhead);
 
-  // Window element i is row base - 1 + i.
-  for (int i = tid; i < kWindow; i += kBuildThreads) {
-    const uint64_t g = base + i - 1;  // wraps to 2^64-1 for row -1: excluded
-    if (g < n) {
-      sm.v[pad_idx(i)] = sv[g];
-      sm.r[pad_idx(i)] = sr ? sr[g] : (uint32_t)g;
+  // This thread's rows: first .. first+7 of the tile, in registers.
+  const uint32_t first = tid * kBuildItems;
+  uint32_t v[kBuildItems], cb[kBuildItems];
+  if (full) {
+    const uint4* v4 = reinterpret_cast<const uint4*>(sv + base + first);
+    const uint4 a0 = v4[0], a1 = v4[1];
+    v[0] = a0.x; v[1] = a0.y; v[2] = a0.z; v[3] = a0.w;
+    v[4] = a1.x; v[5] = a1.y; v[6] = a1.z; v[7] = a1.w;
+    if (sr) {
+      const uint4* r4 = reinterpret_cast<const uint4*>(sr + base + first);
+      const uint4 b0 = r4[0], b1 = r4[1];
+      cb[0] = chunk_bit(b0.x); cb[1] = chunk_bit(b0.y); cb[2] = chunk_bit(b0.z);
+      cb[3] = chunk_bit(b0.w); cb[4] = chunk_bit(b1.x); cb[5] = chunk_bit(b1.y);
+      cb[6] = chunk_bit(b1.z); cb[7] = chunk_bit(b1.w);
+    } else {
+#pragma unroll
+      for (int j = 0; j < kBuildItems; ++j) cb[j] = chunk_bit((uint32_t)base + first + j);
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < kBuildItems; ++j) {
+      const bool ok = first + j < valid;
+      v[j] = ok ? sv[base + first + j] : 0u;
+      const uint32_t r = ok ? (sr ? sr[base + first + j] : (uint32_t)base + first + j) : 0u;
+      cb[j] = chunk_bit(r);
+    }
+  }
+  {
+    uint4* wv = reinterpret_cast<uint4*>(&sm.v[first]);
+    uint4* wc = reinterpret_cast<uint4*>(&sm.cb[first]);
+    wv[0] = make_uint4(v[0], v[1], v[2], v[3]);
+    wv[1] = make_uint4(v[4], v[5], v[6], v[7]);
+    wc[0] = make_uint4(cb[0], cb[1], cb[2], cb[3]);
+    wc[1] = make_uint4(cb[4], cb[5], cb[6], cb[7]);
+  }
+  // Look-ahead rows (segments that start in this tile end inside them).
+  if (tid < kLookAhead) {
+    const uint32_t i = kBuildTile + tid;
+    if (i < wend) {
+      sm.v[i] = sv[base + i];
+      sm.cb[i] = chunk_bit(sr ? sr[base + i] : (uint32_t)(base + i));
+    }
+  }
+  // Look-behind row: the last row of the previous tile, or, for the first
+  // tile, a value that differs from row 0 (so row 0 heads a new key).
+  if (tid == kBuildThreads - 1) {
+    if (base > 0) {
+      sm.prev_v = sv[base - 1];
+      sm.prev_cb = chunk_bit(sr ? sr[base - 1] : (uint32_t)(base - 1));
+    } else {
+      sm.prev_v = ~sv[0];
+      sm.prev_cb = 0;
     }
   }
   __syncthreads();
 
-  // Classify this thread's rows: rows tid*ITEMS .. +ITEMS-1 of the tile.
-  const uint32_t first = tid * kBuildItems;
-  uint32_t my_words = 0, my_keys = 0, my_segs = 0;
+  // Classify rows: head of a (value, chunk) segment / head of a value.
+  uint32_t pv = tid ? sm.v[first - 1] : sm.prev_v;
+  uint32_t pc = (tid ? sm.cb[first - 1] : sm.prev_cb) >> 5;
+  uint32_t headm = 0, vheadm = 0, fills[kBuildItems];
+  uint32_t nw = 0;
 #pragma unroll
   for (int j = 0; j < kBuildItems; ++j) {
-    const uint32_t li = first + j;
-    const uint64_t g = base + li;
-    if (g < n) {
-      const uint32_t v = sm.v[pad_idx(li + 1)];
-      const uint32_t c = sm.r[pad_idx(li + 1)] / 31;
-      bool vhead = true, head = true;
-      uint32_t fill = c;
-      if (g > 0) {
-        const uint32_t vp = sm.v[pad_idx(li)];
-        const uint32_t cp = sm.r[pad_idx(li)] / 31;
-        vhead = v != vp;
-        head = vhead || c != cp;
-        if (!vhead) fill = c - cp - 1;
-      }
-      if (head) {
-        my_words += 1 + (fill != 0);
-        my_keys += vhead;
-        my_segs += 1;
-      }
+    const uint32_t c = cb[j] >> 5;
+    const bool ok = full || first + j < valid;
+    const bool vh = v[j] != pv;
+    const bool h = ok && (vh || c != pc);
+    fills[j] = vh ? c : c - pc - 1;
+    if (h) {
+      headm |= 1u << j;
+      if (vh) vheadm |= 1u << j;
+      nw += 1 + (fills[j] != 0);
+    }
+    pv = v[j];
+    pc = c;
+  }
+  const uint32_t nk = __popc(vheadm), ns = __popc(headm);
+
+  // Literals: reverse segmented OR.  First the rows after this thread's last
+  // row that continue its last segment (from shared memory), then backwards.
+  uint32_t acc = 0;
+  {
+    const uint32_t c7 = cb[kBuildItems - 1] >> 5;
+    for (uint32_t m = first + kBuildItems; m < wend; ++m) {
+      if (sm.v[m] != v[kBuildItems - 1] || (sm.cb[m] >> 5) != c7) break;
+      acc |= 1u << (sm.cb[m] & 31);
     }
   }
-
-  // Block scan of the packed (keys << 32 | words) counters.
-  uint64_t tile_agg;
-  const uint64_t my_prefix = block_exclusive_scan64<kBuildThreads>(
-      ((uint64_t)my_keys << 32) | my_words, &tile_agg, sm.warp_tmp);
-
-  // Merged-entry count k for the caller (one atomic per tile).
-  {
-    uint32_t segs_total;
-    __shared__ uint32_t s_segs_warp[kBuildThreads / 32 + 1];
-    block_exclusive_scan<kBuildThreads>(my_segs, &segs_total, s_segs_warp);
-    if (tid == 0 && segs_total) atomicAdd(&counts->merged, segs_total);
+  uint32_t lits[kBuildItems];
+#pragma unroll
+  for (int j = kBuildItems - 1; j >= 0; --j) {
+    if (full || first + j < valid) acc |= 1u << (cb[j] & 31);  // rows past n add nothing
+    lits[j] = acc | 0x80000000u;
+    if (headm & (1u << j)) acc = 0;
   }
 
-  // Look-back: warp 0 publishes the aggregate, waits for the prefix.
+  uint64_t tile_agg;
+  const uint64_t my_prefix = block_exclusive_scan64<kBuildThreads>(
+      (uint64_t)nw | ((uint64_t)nk << kPackShift) | ((uint64_t)ns << (2 * kPackShift)), &tile_agg,
+      sm.warp_tmp);
+  const uint32_t tw = (uint32_t)(tile_agg & kPackMask);
+  const uint32_t tk = (uint32_t)((tile_agg >> kPackShift) & kPackMask);
+  const uint32_t ts = (uint32_t)(tile_agg >> (2 * kPackShift));
+
+  if (tid == 0 && ts) atomicAdd(&counts->merged, ts);
   if (tid < 32) {
+    const uint64_t agg = ((uint64_t)tk << 32) | tw;
     uint64_t* lbt = lb + tile;
     uint64_t excl = 0;
     if (tile == 0) {
-      if (tid == 0) st_relaxed_u64(lbt, kLbPrefix64 | tile_agg);
+      if (tid == 0) st_relaxed_u64(lbt, kLbPrefix64 | agg);
     } else {
-      if (tid == 0) st_relaxed_u64(lbt, kLbAggregate64 | tile_agg);
+      if (tid == 0) st_relaxed_u64(lbt, kLbAggregate64 | agg);
       excl = build_lookback(lb, tile, status, &sm.abort);
-      if (tid == 0) st_relaxed_u64(lbt, kLbPrefix64 | (excl + tile_agg));
+      if (tid == 0) st_relaxed_u64(lbt, kLbPrefix64 | (excl + agg));
     }
     if (tid == 0) sm.tile_prefix = excl;
+  }
+
+  // Stage this thread's words, keys and offsets (tile-local positions).
+  uint32_t pw = (uint32_t)(my_prefix & kPackMask);
+  uint32_t pk = (uint32_t)((my_prefix >> kPackShift) & kPackMask);
+#pragma unroll
+  for (int j = 0; j < kBuildItems; ++j) {
+    if (headm & (1u << j)) {
+      if (vheadm & (1u << j)) {
+        sm.keys[skew(pk)] = v[j];
+        sm.offs[skew(pk)] = pw;  // tile-local; the tile's word prefix is added below
+        ++pk;
+      }
+      if (fills[j]) sm.words[skew(pw++)] = fills[j];
+      sm.words[skew(pw++)] = lits[j];
+    }
   }
   __syncthreads();
   if (sm.abort) return;
   const uint64_t tile_prefix = sm.tile_prefix;
-  const uint32_t xw = (uint32_t)(tile_prefix & 0xffffffffu);  // words before tile
-  const uint32_t xk = (uint32_t)(tile_prefix >> 32);          // keys before tile
+  const uint32_t xw = (uint32_t)(tile_prefix & 0xffffffffu);
+  const uint32_t xk = (uint32_t)(tile_prefix >> 32);
 
-  // Emit: words into shared staging, keys/offsets straight to global.
-  uint32_t pw = (uint32_t)(my_prefix & 0xffffffffu);
-  uint32_t pk = (uint32_t)(my_prefix >> 32);
   bool overflow = false;
-#pragma unroll
-  for (int j = 0; j < kBuildItems; ++j) {
-    const uint32_t li = first + j;
-    const uint64_t g = base + li;
-    if (g < n) {
-      const uint32_t v = sm.v[pad_idx(li + 1)];
-      const uint32_t r = sm.r[pad_idx(li + 1)];
-      const uint32_t c = r / 31;
-      bool vhead = true, head = true;
-      uint32_t fill = c;
-      if (g > 0) {
-        const uint32_t vp = sm.v[pad_idx(li)];
-        const uint32_t cp = sm.r[pad_idx(li)] / 31;
-        vhead = v != vp;
-        head = vhead || c != cp;
-        if (!vhead) fill = c - cp - 1;
-      }
-      if (head) {
-        // OR the segment's rows (at most 31, all inside the window).
-        uint32_t lit = 0x80000000u | (1u << (r % 31));
-        for (uint32_t m = li + 1; m < li + 31 && base + m < n; ++m) {
-          const uint32_t rm = sm.r[pad_idx(m + 1)];
-          if (sm.v[pad_idx(m + 1)] != v || rm / 31 != c) break;
-          lit |= 1u << (rm % 31);
-        }
-        if (vhead) {
-          const uint64_t kpos = (uint64_t)xk + pk;
-          if (kpos < keys_cap) {
-            keys[kpos] = v;
-            offsets[kpos] = xw + pw;
-          } else {
-            overflow = true;
-          }
-          ++pk;
-        }
-        if (fill) sm.words[pw++] = fill;
-        sm.words[pw++] = lit;
-      }
-    }
-  }
-  __syncthreads();
-
-  // Coalesced write of the tile's words.
-  const uint32_t tw = (uint32_t)(tile_agg & 0xffffffffu);
   for (uint32_t i = tid; i < tw; i += kBuildThreads) {
     const uint64_t pos = (uint64_t)xw + i;
     if (pos < index_cap)
-      index[pos] = sm.words[i];
+      index[pos] = sm.words[skew(i)];
     else
       overflow = true;
+  }
+  for (uint32_t i = tid; i < tk; i += kBuildThreads) {
+    const uint64_t pos = (uint64_t)xk + i;
+    if (pos < keys_cap) {
+      keys[pos] = sm.keys[skew(i)];
+      offsets[pos] = xw + sm.offs[skew(i)];
+    } else {
+      overflow = true;
+    }
   }
   if (overflow) set_status(status, WAH_EOVERFLOW);
 
   // The last tile knows the totals.
   if (tid == 0 && base + kBuildTile >= n) {
-    const uint64_t tot = tile_prefix + tile_agg;
+    const uint64_t tot = tile_prefix + (((uint64_t)tk << 32) | tw);
     counts->index_len = (uint32_t)(tot & 0xffffffffu);
     counts->keycnt = (uint32_t)(tot >> 32);
   }

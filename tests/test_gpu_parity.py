@@ -125,3 +125,22 @@ def test_decoded_bitmaps_match_rows(wah):
         rows = np.flatnonzero(v == idx.keys[i])
         s = wah.decoded_bitmap(idx.bitmap(i))
         assert [j for j, ch in enumerate(s) if ch == "1"] == rows.tolist()
+
+
+@pytest.mark.parametrize("items", [8, 12, 16, 20])
+def test_every_sort_tile_shape(wah, items):
+    lib = wah._lib.load()
+    old = lib.wah_get_tuning()
+    assert lib.wah_set_tuning(items) == 0
+    try:
+        rng = np.random.default_rng(items)
+        for kind, n in (("uniform16", 300_001), ("u32", 77_777), ("runs", 200_000),
+                        ("few16", 5_003)):
+            v = gen(kind, n, rng)
+            assert_same(wah.build_index(v), O.build(v), f"{kind}/{n}/items{items}")
+    finally:
+        lib.wah_set_tuning(old)
+
+
+def test_rejects_unknown_tuning(wah):
+    assert wah._lib.load().wah_set_tuning(7) == wah.WAH_EINVAL
