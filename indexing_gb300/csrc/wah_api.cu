@@ -14,13 +14,14 @@ namespace wah {
 namespace {
 
 thread_local uint32_t g_last_launches = 0;
-int g_sort_items = 16;  // onesweep rows per thread (wah_set_tuning)
+int g_sort_items = 16;      // onesweep rows per thread (wah_set_tuning)
+bool g_sort_ballot = true;  // peer masks from ballots (wah_set_tuning)
 
 constexpr size_t kAlign = 256;
 inline size_t align_up(size_t x) { return (x + kAlign - 1) / kAlign * kAlign; }
 
 struct WsLayout {
-  size_t ctrl, lb_sort, lb_build, keys_a, rids_a, keys_b, rids_b, total;
+  size_t ctrl, range_hist, range_start, lb_build, keys_a, rids_a, keys_b, rids_b, total;
 };
 
 WsLayout ws_layout(uint64_t n) {
@@ -28,9 +29,10 @@ WsLayout ws_layout(uint64_t n) {
   size_t off = 0;
   l.ctrl = off;
   off += align_up(sizeof(WahCtrl));
-  l.lb_sort = off;
-  off += align_up(ceil_div(std::max<uint64_t>(n, 1), (uint64_t)kSortThreads * kSortMinItems) *
-                  kRadix * sizeof(uint32_t));
+  l.range_hist = off;
+  off += align_up((size_t)kDigits * kMaxRanges * kRadix * sizeof(uint32_t));
+  l.range_start = off;
+  off += align_up((size_t)kMaxRanges * kRadix * sizeof(uint32_t));
   l.lb_build = off;
   off += align_up(ceil_div(std::max<uint64_t>(n, 1), kBuildTile) * sizeof(uint64_t));
   const size_t col = align_up(std::max<uint64_t>(n, 1) * sizeof(uint32_t));
@@ -87,7 +89,8 @@ int enqueue_sort(const uint32_t* d_values, uint64_t n, uint32_t bound, const WsL
   a.n = n;
   a.passes = passes_for_bound(bound);
   a.ctrl = ctrl;
-  a.lb_sort = reinterpret_cast<uint32_t*>(ws + l.lb_sort);
+  a.range_hist = reinterpret_cast<uint32_t*>(ws + l.range_hist);
+  a.range_start = reinterpret_cast<uint32_t*>(ws + l.range_start);
   a.buf_keys[0] = reinterpret_cast<uint32_t*>(ws + l.keys_a);
   a.buf_rids[0] = reinterpret_cast<uint32_t*>(ws + l.rids_a);
   a.buf_keys[1] = reinterpret_cast<uint32_t*>(ws + l.keys_b);
@@ -95,6 +98,7 @@ int enqueue_sort(const uint32_t* d_values, uint64_t n, uint32_t bound, const WsL
   a.status = status;
   a.events = events;
   a.sort_items = g_sort_items;
+  a.sort_ballot = g_sort_ballot;
   a.sm_count = sm_count_current();
   if (a.sm_count <= 0) return WAH_ENODEV;
   e = launch_sort(a, s, launches);
@@ -141,13 +145,14 @@ size_t wah_workspace_bytes(uint64_t n, uint32_t /*bound*/) { return ws_layout(n)
 uint32_t wah_last_launch_count(void) { return g_last_launches; }
 
 int wah_set_tuning(int sort_items) {
-  if (sort_items != 8 && sort_items != 12 && sort_items != 16 && sort_items != 20)
-    return WAH_EINVAL;
-  g_sort_items = sort_items;
+  const int items = sort_items & 0xff;
+  if (items != 8 && items != 12 && items != 16) return WAH_EINVAL;
+  g_sort_items = items;
+  g_sort_ballot = !(sort_items & WAH_TUNE_MATCH);
   return WAH_OK;
 }
 
-int wah_get_tuning(void) { return g_sort_items; }
+int wah_get_tuning(void) { return g_sort_items | (g_sort_ballot ? 0 : WAH_TUNE_MATCH); }
 
 static int build_impl(const uint32_t* d_values, uint64_t n, uint32_t bound, uint32_t* d_keys,
                       uint32_t* d_offsets, uint32_t* d_index, wah_counts* d_counts,

@@ -19,10 +19,18 @@ constexpr int kRadixBits = 8;
 constexpr int kRadix = 1 << kRadixBits;  // 256 bins per digit
 constexpr int kDigits = 4;               // 32-bit keys -> up to 4 passes
 
-// Onesweep pass: 256 threads (one per bin in the look-back); rows per thread
-// is a tuning choice (8/12/16/20), kSortMinItems bounds the look-back array.
+// Radix scatter: 256 threads (one per bin), rows per thread a tuning choice
+// (8/12/16).  The column is cut into at most kMaxRanges equal row ranges, one
+// persistent scatter CTA each; histogram/count kernels use
+// kCountCtasPerRange CTAs per range.
 constexpr int kSortThreads = 256;
-constexpr int kSortMinItems = 8;
+constexpr int kMaxRanges = 1024;
+constexpr int kCountCtasPerRange = 2;
+
+struct RangeGeom {
+  uint64_t range_rows;  // rows per range, a multiple of the scatter tile
+  uint32_t ranges;      // number of ranges (<= kMaxRanges)
+};
 
 // Fused index build: 256 threads x 8 rows, blocked.
 constexpr int kBuildThreads = 256;
@@ -119,6 +127,56 @@ __device__ __forceinline__ uint32_t bfe(uint32_t x, uint32_t pos, uint32_t len) 
   return r;
 }
 
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+// mbarrier + bulk-copy (TMA, non-tensor) helpers.
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+               : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+// Orders this thread's (and, after a barrier, the block's) generic-proxy
+// shared-memory accesses before later async-proxy (bulk copy) writes.
+__device__ __forceinline__ void fence_proxy_async_shared() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+// Global -> shared bulk copy; both addresses 16-byte aligned, bytes % 16 == 0.
+__device__ __forceinline__ void bulk_copy_g2s(void* dst, const void* src, uint32_t bytes,
+                                              uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+          "r"(smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait for a phase of an mbarrier; false after kSpinLimit polls.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+  for (uint32_t i = 0; i < kSpinLimit; ++i) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (i > kSpinFast) __nanosleep(64);
+  }
+  return false;
+}
+
 // First error wins.
 __device__ __forceinline__ void set_status(uint32_t* status, uint32_t code) {
   if (status) atomicCAS(status, 0u, code);
@@ -206,15 +264,17 @@ struct SortLaunch {
   uint64_t n;
   int passes;  // digit passes to launch (1..4)
   WahCtrl* ctrl;
-  uint32_t* lb_sort;  // tiles * 256 u32
+  uint32_t* range_hist;   // [kDigits][kMaxRanges][256] u32, zeroed per build
+  uint32_t* range_start;  // [kMaxRanges][256] u32
   uint32_t* buf_keys[2];
   uint32_t* buf_rids[2];
   uint32_t* status;
   int sm_count;
   int sort_items;       // onesweep rows per thread (8, 12, 16, 20)
+  bool sort_ballot;     // peer masks from ballots instead of match.any
   cudaEvent_t* events;  // optional: [2*phase] before, [2*phase+1] after
 };
-uint64_t sort_tiles(uint64_t n, int items);
+
 cudaError_t launch_sort(const SortLaunch& a, cudaStream_t s, uint32_t* launches);
 cudaError_t launch_sort_deliver(const SortBufs& bufs, const WahCtrl* ctrl, uint64_t n,
                                 uint32_t* out_keys, uint32_t* out_rids, cudaStream_t s,

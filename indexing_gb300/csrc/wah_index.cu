@@ -74,7 +74,7 @@ __device__ __forceinline__ uint64_t build_lookback(uint64_t* __restrict__ lb, ui
         }
         break;
       }
-      if (spins > kSpinFast) __nanosleep(128);
+      __nanosleep(spins > kSpinFast ? 256 : 32);
       continue;
     }
     const uint32_t pmask = __ballot_sync(0xffffffffu, fl == 2);
@@ -226,21 +226,11 @@ __global__ void __launch_bounds__(kBuildThreads, 4)
   const uint32_t ts = (uint32_t)(tile_agg >> (2 * kPackShift));
 
   if (tid == 0 && ts) atomicAdd(&counts->merged, ts);
-  if (tid < 32) {
-    const uint64_t agg = ((uint64_t)tk << 32) | tw;
-    uint64_t* lbt = lb + tile;
-    uint64_t excl = 0;
-    if (tile == 0) {
-      if (tid == 0) st_relaxed_u64(lbt, kLbPrefix64 | agg);
-    } else {
-      if (tid == 0) st_relaxed_u64(lbt, kLbAggregate64 | agg);
-      excl = build_lookback(lb, tile, status, &sm.abort);
-      if (tid == 0) st_relaxed_u64(lbt, kLbPrefix64 | (excl + agg));
-    }
-    if (tid == 0) sm.tile_prefix = excl;
-  }
+  const uint64_t agg = ((uint64_t)tk << 32) | tw;
+  if (tid == 0) st_relaxed_u64(lb + tile, (tile == 0 ? kLbPrefix64 : kLbAggregate64) | agg);
 
-  // Stage this thread's words, keys and offsets (tile-local positions).
+  // Stage this thread's words, keys and offsets at tile-local positions
+  // (before the look-back, which then finds its predecessors published).
   uint32_t pw = (uint32_t)(my_prefix & kPackMask);
   uint32_t pk = (uint32_t)((my_prefix >> kPackShift) & kPackMask);
 #pragma unroll
@@ -254,6 +244,14 @@ __global__ void __launch_bounds__(kBuildThreads, 4)
       if (fills[j]) sm.words[skew(pw++)] = fills[j];
       sm.words[skew(pw++)] = lits[j];
     }
+  }
+  if (tid < 32) {
+    uint64_t excl = 0;
+    if (tile > 0) {
+      excl = build_lookback(lb, tile, status, &sm.abort);
+      if (tid == 0) st_relaxed_u64(lb + tile, kLbPrefix64 | (excl + agg));
+    }
+    if (tid == 0) sm.tile_prefix = excl;
   }
   __syncthreads();
   if (sm.abort) return;

@@ -1,21 +1,29 @@
-// wah_sort.cu -- phase a1, sort_rids_by_value, as a stable onesweep LSD radix
-// sort carrying row ids.
+// wah_sort.cu -- phase a1, sort_rids_by_value: a stable LSD radix sort of the
+// column by value, carrying row ids, with 8-bit digits.
 //
 // Reference semantics: src/cpu.cpp:180-197 (stable bubble sort by value,
 // rids = iota) and src/phases.cpp:143-160 (the same as std::stable_sort).
 // The reference GPU path (src/phases.cpp:745-773 over include/radix.cl:65-233)
 // runs 4 passes x (count, scan, reorder_kv) of 4-bit digits over the low 16
-// bits only.  Here:
-//   k_digit_histogram  one read of the keys builds the histograms of all four
-//                      8-bit digits (128-bit loads; per-thread run-length
-//                      counting so constant digits cost no shared atomics)
-//   k_sort_plan        scans the histograms into global bin offsets and plans
-//                      the passes: a digit whose values all fall in one bin is
-//                      skipped (the stable sort by it is the identity)
-//   k_onesweep_pass    one launch per digit: tile load, warp match-based
-//                      stable ranking, decoupled look-back across tiles for
-//                      each bin's global offset, staged scatter.  The first
-//                      active pass takes rid = row index (no iota kernel).
+// bits only.  Here the column is cut into R equal row ranges (R = resident
+// scatter CTAs); each range is owned by one persistent CTA, so no CTA ever
+// waits for another:
+//
+//   k_digit_histogram  one read of the keys (128-bit loads): histograms of
+//                      every digit the bound allows for the whole column, the
+//                      digit-0 histogram per range, and the OR of all keys
+//   k_sort_plan        bin offsets per digit, trivial digits skipped, homes
+//                      of each pass
+//   k_range_count      for digit passes after the first: per-range histogram
+//                      of the digit over the current order (one read of keys)
+//   k_range_scan       start of every (range, bin) = bin offset + counts of
+//                      the same bin in earlier ranges
+//   k_radix_scatter    per range, tile after tile: the next tile's keys and
+//                      row ids are fetched by cp.async.bulk into shared memory
+//                      while this one is ranked (warp peer masks, stable per
+//                      warp counters), staged in tile-sorted order and written
+//                      out run by run at the range's running bin offsets.  The
+//                      first active pass takes rid = row index.
 #include <algorithm>
 
 #include "wah_common.cuh"
@@ -23,16 +31,15 @@
 namespace wah {
 
 // ---------------------------------------------------------------------------
-// Digit histograms.  Keys are read once with 128-bit loads.  Per warp and key
-// slot, a digit whose 8 bits agree across all 32 lanes (found from the warp's
-// OR and AND of the keys) is counted with one shared atomic for the warp
-// instead of 32: constant high digits of small keys and runs of equal values
-// cost almost nothing.  DIGITS is the number of digit passes the bound allows;
-// the OR of all keys is kept so the plan can flag values above the bound.
+// Digit histograms.  Per warp and key slot, a digit whose 8 bits agree across
+// all 32 lanes (found from the warp's OR and AND of the keys) is counted with
+// one shared atomic for the warp instead of 32: constant high digits of small
+// keys and runs of equal values cost almost nothing.
 // ---------------------------------------------------------------------------
 template <int DIGITS>
 struct WarpHist {
   uint32_t (*h)[kRadix];  // this warp's private [DIGITS][256] counters
+  int first;              // digit of h[0]
   __device__ __forceinline__ void add_full_warp(uint32_t x, uint32_t lane, uint32_t& acc_or) {
     const uint32_t o = __reduce_or_sync(0xffffffffu, x);
     const uint32_t a = __reduce_and_sync(0xffffffffu, x);
@@ -40,8 +47,9 @@ struct WarpHist {
     const uint32_t varying = o ^ a;
 #pragma unroll
     for (int p = 0; p < DIGITS; ++p) {
-      const uint32_t d = bfe(x, p * kRadixBits, kRadixBits);
-      if (bfe(varying, p * kRadixBits, kRadixBits) == 0) {
+      const uint32_t pos = (first + p) * kRadixBits;
+      const uint32_t d = bfe(x, pos, kRadixBits);
+      if (bfe(varying, pos, kRadixBits) == 0) {
         if (lane == 0) atomicAdd(&h[p][d], 32u);
       } else {
         atomicAdd(&h[p][d], 1u);
@@ -51,28 +59,27 @@ struct WarpHist {
   __device__ __forceinline__ void add_one(uint32_t x, uint32_t& acc_or) {
     acc_or |= x;
 #pragma unroll
-    for (int p = 0; p < DIGITS; ++p) atomicAdd(&h[p][bfe(x, p * kRadixBits, kRadixBits)], 1u);
+    for (int p = 0; p < DIGITS; ++p)
+      atomicAdd(&h[p][bfe(x, (first + p) * kRadixBits, kRadixBits)], 1u);
   }
 };
 
+// Histogram of keys[lo, hi) for digits first..first+DIGITS-1 into the
+// block-shared s_h[warp][DIGITS][256]; returns the warp's OR of the keys.
 template <int DIGITS>
-__global__ void __launch_bounds__(kHistThreads)
-    k_digit_histogram(const uint32_t* __restrict__ keys, uint64_t n, WahCtrl* ctrl) {
-  __shared__ uint32_t s_h[kHistWarps][DIGITS][kRadix];
-  for (int i = threadIdx.x; i < kHistWarps * DIGITS * kRadix; i += kHistThreads)
-    (&s_h[0][0][0])[i] = 0;
-  __syncthreads();
-
+__device__ __forceinline__ uint32_t histogram_range(const uint32_t* __restrict__ keys, uint64_t lo,
+                                                    uint64_t hi, int first,
+                                                    uint32_t (*s_h)[DIGITS][kRadix]) {
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  WarpHist<DIGITS> wh{s_h[warp]};
+  const uint32_t nwarps = blockDim.x >> 5;
+  WarpHist<DIGITS> wh{s_h[warp], first};
   uint32_t acc_or = 0;
-  // Work unit: a chunk of 32 consecutive uint4 (512 keys), one per lane.
-  const uint64_t n4 = n / 4;
-  const uint64_t chunks = n4 / 32;  // full chunks
-  const uint4* kv = reinterpret_cast<const uint4*>(keys);
-  const uint64_t gwarp = (uint64_t)blockIdx.x * kHistWarps + warp;
-  const uint64_t nwarps = (uint64_t)gridDim.x * kHistWarps;
-  uint64_t c = gwarp;
+  // lo is a multiple of 4 (ranges are whole tiles), so keys + lo is 16-byte
+  // aligned.  Work unit: 32 consecutive uint4 (128 keys), one per lane.
+  const uint4* kv = reinterpret_cast<const uint4*>(keys + lo);
+  const uint64_t rows = hi - lo;
+  const uint64_t chunks = rows / 128;
+  uint64_t c = warp;
   for (; c + (kHistUnroll - 1) * nwarps < chunks; c += kHistUnroll * nwarps) {
     uint4 q[kHistUnroll];
 #pragma unroll
@@ -92,18 +99,69 @@ __global__ void __launch_bounds__(kHistThreads)
     wh.add_full_warp(q.z, lane, acc_or);
     wh.add_full_warp(q.w, lane, acc_or);
   }
-  // Ragged end (< 512 keys): the first warp of the grid, one key per lane.
-  if (gwarp == 0) {
-    for (uint64_t i = chunks * 128 + lane; i < n; i += 32) wh.add_one(keys[i], acc_or);
-  }
-  acc_or = __reduce_or_sync(0xffffffffu, acc_or);
-  if (lane == 0 && acc_or) atomicOr(&ctrl->key_or, acc_or);
+  // Ragged end (< 128 keys): warp 0, one key per lane.
+  if (warp == 0)
+    for (uint64_t i = lo + chunks * 128 + lane; i < hi; i += 32) wh.add_one(keys[i], acc_or);
+  return __reduce_or_sync(0xffffffffu, acc_or);
+}
+
+// Sub-range q of range c: the rows one histogram CTA covers.
+__device__ __forceinline__ void sub_range(const RangeGeom& g, uint64_t n, uint32_t cta,
+                                          uint64_t* lo, uint64_t* hi) {
+  const uint32_t c = cta / kCountCtasPerRange, q = cta % kCountCtasPerRange;
+  const uint64_t part = g.range_rows / kCountCtasPerRange;  // multiple of 4
+  const uint64_t a = (uint64_t)c * g.range_rows + q * part;
+  const uint64_t b = q + 1 == kCountCtasPerRange ? (uint64_t)(c + 1) * g.range_rows : a + part;
+  *lo = a < n ? a : n;
+  *hi = b < n ? b : n;
+}
+
+template <int DIGITS>
+__global__ void __launch_bounds__(kHistThreads)
+    k_digit_histogram(const uint32_t* __restrict__ keys, uint64_t n, RangeGeom g, WahCtrl* ctrl,
+                      uint32_t* __restrict__ range_hist0) {
+  __shared__ uint32_t s_h[kHistWarps][DIGITS][kRadix];
+  for (int i = threadIdx.x; i < kHistWarps * DIGITS * kRadix; i += kHistThreads)
+    (&s_h[0][0][0])[i] = 0;
   __syncthreads();
+  uint64_t lo, hi;
+  sub_range(g, n, blockIdx.x, &lo, &hi);
+  const uint32_t acc_or = histogram_range<DIGITS>(keys, lo, hi, 0, s_h);
+  if ((threadIdx.x & 31) == 0 && acc_or) atomicOr(&ctrl->key_or, acc_or);
+  __syncthreads();
+  const uint32_t c = blockIdx.x / kCountCtasPerRange;
   for (int j = threadIdx.x; j < DIGITS * kRadix; j += kHistThreads) {
-    uint32_t c2 = 0;
+    uint32_t s = 0;
 #pragma unroll
-    for (int w = 0; w < kHistWarps; ++w) c2 += (&s_h[w][0][0])[j];
-    if (c2) atomicAdd(&(&ctrl->hist[0][0])[j], c2);
+    for (int w = 0; w < kHistWarps; ++w) s += (&s_h[w][0][0])[j];
+    if (s) {
+      atomicAdd(&(&ctrl->hist[0][0])[j], s);
+      if (j < kRadix) atomicAdd(&range_hist0[(uint64_t)c * kRadix + j], s);
+    }
+  }
+}
+
+// Per-range histogram of digit `pass` over the current order of the keys.
+__global__ void __launch_bounds__(kHistThreads)
+    k_range_count(const uint32_t* input, const uint32_t* keys_a, const uint32_t* keys_b,
+                  uint64_t n, RangeGeom g, int pass, const WahCtrl* ctrl,
+                  uint32_t* __restrict__ range_hist) {
+  const int src = ctrl->pass_src[pass];
+  if (src < 0) return;
+  const uint32_t* keys = src == kSelInput ? input : (src == kSelA ? keys_a : keys_b);
+  __shared__ uint32_t s_h[kHistWarps][1][kRadix];
+  for (int i = threadIdx.x; i < kHistWarps * kRadix; i += kHistThreads) (&s_h[0][0][0])[i] = 0;
+  __syncthreads();
+  uint64_t lo, hi;
+  sub_range(g, n, blockIdx.x, &lo, &hi);
+  histogram_range<1>(keys, lo, hi, pass, s_h);
+  __syncthreads();
+  const uint32_t c = blockIdx.x / kCountCtasPerRange;
+  for (int j = threadIdx.x; j < kRadix; j += kHistThreads) {
+    uint32_t s = 0;
+#pragma unroll
+    for (int w = 0; w < kHistWarps; ++w) s += s_h[w][0][j];
+    if (s) atomicAdd(&range_hist[(uint64_t)c * kRadix + j], s);
   }
 }
 
@@ -144,286 +202,370 @@ __global__ void __launch_bounds__(kRadix)
   }
 }
 
+// Start of every (range, bin) for one pass.
+__global__ void __launch_bounds__(kRadix)
+    k_range_scan(const WahCtrl* ctrl, int pass, uint32_t ranges,
+                 const uint32_t* __restrict__ range_hist, uint32_t* __restrict__ range_start) {
+  if (ctrl->pass_src[pass] < 0) return;
+  const uint32_t b = threadIdx.x;
+  uint32_t run = ctrl->bin_off[pass][b];
+  uint32_t c = 0;
+  for (; c + 8 <= ranges; c += 8) {
+    uint32_t h[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) h[u] = range_hist[(uint64_t)(c + u) * kRadix + b];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      range_start[(uint64_t)(c + u) * kRadix + b] = run;
+      run += h[u];
+    }
+  }
+  for (; c < ranges; ++c) {
+    range_start[(uint64_t)c * kRadix + b] = run;
+    run += range_hist[(uint64_t)c * kRadix + b];
+  }
+}
+
 // ---------------------------------------------------------------------------
-// One onesweep digit pass over tiles of 4096 rows (256 threads x 16).
+// Range scatter: one persistent CTA per range, 256 threads x ITEMS rows per
+// tile.
 //
-//  load     warp-striped: item j of lane l in warp w is tile row
-//           w*512 + j*32 + l, so a warp's item-j load is one 128-byte line;
-//           (j, l) order is row order, which makes the ranking stable
-//  rank     all 16 peer masks first (__match_any_sync, independent, so their
-//           latency overlaps), then per item one shared read of the warp's
-//           bin counter, a leader update and a popcount
-//  publish  per-bin tile counts as look-back aggregates, then a per-bin
-//           decoupled look-back (thread b walks bin b) for the global offset
-//  scatter  rows to shared memory in tile-sorted order, then written out by
-//           consecutive threads to consecutive positions of each bin run
+//  fetch    cp.async.bulk of the next tile's keys (and row ids) into the other
+//           half of a double buffer, completion on an mbarrier
+//  rank     warp-striped rows (item j of lane l in warp w is tile row
+//           w*32*ITEMS + j*32 + l, so (j, l) order is row order); peer masks
+//           (lanes holding the same digit) from eight ballots or
+//           __match_any_sync; two independent per-warp counter chains (first
+//           and second half of the warp's rows) give stable warp ranks
+//  stage    rows in tile-sorted order in shared memory
+//  write    consecutive threads to consecutive positions of each bin run, at
+//           the range's running bin offsets, which then advance by the
+//           tile's counts
 // ---------------------------------------------------------------------------
 constexpr int kSortWarps = kSortThreads / 32;
-static_assert(kSortThreads == kRadix, "one thread per bin in the look-back");
+static_assert(kSortThreads == kRadix, "one thread per bin");
 
+// The tile-sorted keys are staged in the input key buffer the tile came from
+// (its keys are in registers by then); row ids need their own staging.
 template <int ITEMS>
-struct SortPassSmem {
-  uint32_t whist[kSortWarps][kRadix];  // per-warp counts -> tile-local starts
-  uint32_t bin_base[kRadix];           // global position - tile-local start
+struct ScatterSmem {
+  uint32_t in_keys[2][kSortThreads * ITEMS];
+  uint32_t in_rids[2][kSortThreads * ITEMS];
+  uint32_t out_rids[kSortThreads * ITEMS];
+  uint32_t whist[kSortWarps][2][kRadix];  // per-warp, per-half counters
+  uint32_t run_off[kRadix];               // range's next free position per bin
+  uint32_t bin_base[kRadix];              // run_off - tile-local bin start
   uint32_t warp_tmp[kSortWarps + 1];
-  uint32_t tile;
+  uint64_t bar[2];
   int abort;
-  uint32_t keys[kSortThreads * ITEMS];
-  uint32_t rids[kSortThreads * ITEMS];
 };
 
-struct SortPassArgs {
+struct ScatterArgs {
   const uint32_t* input;  // selector kSelInput (rid = row index)
   uint32_t* keys_a;
   uint32_t* rids_a;
   uint32_t* keys_b;
   uint32_t* rids_b;
   uint64_t n;
+  RangeGeom g;
   int pass;
-  WahCtrl* ctrl;
-  uint32_t* lookback;
+  const WahCtrl* ctrl;
+  const uint32_t* range_start;  // [ranges][256]
   uint32_t* status;
 };
 
-// Rows past n in the last tile are padded with key 0xFFFFFFFF: digit 255 in
-// every pass, and since the ranking is stable they land after every real row
-// of bin 255, which is the last bin -- i.e. at tile-local positions >= the
-// number of real rows, which are never written out.  Only the last tile's
-// look-back counts include them, and no tile reads those.
-template <int ITEMS>
-__device__ __forceinline__ void onesweep_tile(const SortPassArgs& a, SortPassSmem<ITEMS>& sm,
-                                              const uint32_t* __restrict__ kin,
-                                              const uint32_t* __restrict__ rin,
-                                              uint32_t* __restrict__ kout,
-                                              uint32_t* __restrict__ rout, uint32_t tile,
-                                              uint64_t base) {
-  constexpr uint32_t TILE = kSortThreads * ITEMS;
-  const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const uint32_t shift = a.pass * kRadixBits;
-  const bool full = base + TILE <= a.n;
-  const uint32_t valid = full ? TILE : (uint32_t)(a.n - base);
-  const uint32_t row0 = warp * 32 * ITEMS + lane;  // tile row of item 0
-
-  uint32_t key[ITEMS], rid[ITEMS];
-  {
-    const uint32_t* kp = kin + base + row0;
-    if (full) {
+// Lanes of the warp holding the same 8-bit digit as this lane.
+template <bool BALLOT>
+__device__ __forceinline__ uint32_t digit_peers(uint32_t d) {
+  if (BALLOT) {
+    uint32_t m = 0xffffffffu;
 #pragma unroll
-      for (int j = 0; j < ITEMS; ++j) key[j] = kp[j * 32];
-    } else {
-#pragma unroll
-      for (int j = 0; j < ITEMS; ++j)
-        key[j] = row0 + j * 32 < valid ? kp[j * 32] : 0xffffffffu;
+    for (int bit = 0; bit < kRadixBits; ++bit) {
+      const bool set = (d >> bit) & 1u;
+      const uint32_t bb = __ballot_sync(0xffffffffu, set);
+      m &= set ? bb : ~bb;
     }
-  }
-
-  // Peer masks first (independent), then the sequential counter updates.
-  uint32_t rank[ITEMS];
-#pragma unroll
-  for (int j = 0; j < ITEMS; ++j)
-    rank[j] = __match_any_sync(0xffffffffu, bfe(key[j], shift, kRadixBits));
-  const uint32_t lt = lanemask_lt(), gt = lanemask_gt();
-  uint32_t* wh = sm.whist[warp];
-#pragma unroll
-  for (int j = 0; j < ITEMS; ++j) {
-    const uint32_t peers = rank[j];
-    const uint32_t d = bfe(key[j], shift, kRadixBits);
-    const uint32_t cnt = wh[d];
-    __syncwarp();
-    if ((peers & gt) == 0) wh[d] = cnt + __popc(peers);
-    __syncwarp();
-    rank[j] = cnt + __popc(peers & lt);
-  }
-  // Row ids are loaded only now (registers are free of the peer masks); the
-  // loads overlap the look-back below.
-  if (rin) {
-    const uint32_t* rp = rin + base + row0;
-    if (full) {
-#pragma unroll
-      for (int j = 0; j < ITEMS; ++j) rid[j] = rp[j * 32];
-    } else {
-#pragma unroll
-      for (int j = 0; j < ITEMS; ++j) rid[j] = row0 + j * 32 < valid ? rp[j * 32] : 0u;
-    }
+    return m;
   } else {
-    const uint32_t r0 = (uint32_t)base + row0;
-#pragma unroll
-    for (int j = 0; j < ITEMS; ++j) rid[j] = r0 + j * 32;
-  }
-  __syncthreads();
-
-  // Thread b: the tile's count for bin b, then warp starts within the tile.
-  const uint32_t b = tid;
-  uint32_t count = 0;
-#pragma unroll
-  for (int w = 0; w < kSortWarps; ++w) count += sm.whist[w][b];
-  uint32_t* lb = a.lookback + (uint64_t)tile * kRadix + b;
-  st_relaxed_u32(lb, (tile == 0 ? kLbPrefix32 : kLbAggregate32) | count);
-
-  uint32_t tile_total;
-  const uint32_t lstart = block_exclusive_scan<kSortThreads>(count, &tile_total, sm.warp_tmp);
-  {
-    uint32_t run = lstart;
-#pragma unroll
-    for (int w = 0; w < kSortWarps; ++w) {
-      const uint32_t c = sm.whist[w][b];
-      sm.whist[w][b] = run;
-      run += c;
-    }
-  }
-
-  uint32_t excl = 0;
-  if (tile > 0) {
-    uint32_t k = tile - 1;
-    uint32_t spins = 0;
-    while (true) {
-      const uint32_t e = ld_relaxed_u32(a.lookback + (uint64_t)k * kRadix + b);
-      const uint32_t fl = e >> kLbFlagShift32;
-      if (fl == 0) {
-        if (++spins > kSpinLimit) {
-          set_status(a.status, WAH_ETIMEOUT);
-          sm.abort = 1;
-          break;
-        }
-        if (spins > kSpinFast) __nanosleep(128);
-        continue;
-      }
-      excl += e & kLbMask32;
-      if (fl == 2 || k == 0) break;
-      --k;
-    }
-    st_relaxed_u32(lb, kLbPrefix32 | (excl + count));
-  }
-  sm.bin_base[b] = a.ctrl->bin_off[a.pass][b] + excl - lstart;
-  __syncthreads();
-
-#pragma unroll
-  for (int j = 0; j < ITEMS; ++j) {
-    const uint32_t r = wh[bfe(key[j], shift, kRadixBits)] + rank[j];
-    sm.keys[r] = key[j];
-    sm.rids[r] = rid[j];
-  }
-  __syncthreads();
-  if (sm.abort) return;  // positions unknown: write nothing
-
-  const uint32_t n32 = (uint32_t)a.n;
-#pragma unroll 4
-  for (int it = 0; it < ITEMS; ++it) {
-    const uint32_t i = it * kSortThreads + tid;
-    if (i < valid) {
-      const uint32_t k = sm.keys[i];
-      const uint32_t g = sm.bin_base[bfe(k, shift, kRadixBits)] + i;
-      if (g < n32) {
-        kout[g] = k;
-        rout[g] = sm.rids[i];
-      } else {
-        set_status(a.status, WAH_ETIMEOUT);
-      }
-    }
+    return __match_any_sync(0xffffffffu, d);
   }
 }
 
-template <int ITEMS, int MIN_BLOCKS>
-__global__ void __launch_bounds__(kSortThreads, MIN_BLOCKS) k_onesweep_pass(SortPassArgs a) {
+// Issue the bulk copies of one whole tile (thread 0 only).
+__device__ __forceinline__ void fetch_tile(uint32_t* dst_k, uint32_t* dst_r, uint64_t* bar,
+                                           const uint32_t* kin, const uint32_t* rin,
+                                           uint64_t base, uint32_t rows) {
+  const uint32_t bytes = rows * 4u;
+  fence_proxy_async_shared();
+  mbar_arrive_expect_tx(bar, rin ? 2 * bytes : bytes);
+  bulk_copy_g2s(dst_k, kin + base, bytes, bar);
+  if (rin) bulk_copy_g2s(dst_r, rin + base, bytes, bar);
+}
+
+template <int ITEMS, bool BALLOT>
+__global__ void __launch_bounds__(kSortThreads, 2) k_radix_scatter(ScatterArgs a) {
   constexpr uint32_t TILE = kSortThreads * ITEMS;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  SortPassSmem<ITEMS>& sm = *reinterpret_cast<SortPassSmem<ITEMS>*>(smem_raw);
+  constexpr int HALF = ITEMS / 2;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  ScatterSmem<ITEMS>& sm = *reinterpret_cast<ScatterSmem<ITEMS>*>(smem_raw);
+
   const int src = a.ctrl->pass_src[a.pass];
   if (src < 0) return;  // trivial digit: every row in one bin, order unchanged
   const int dst = a.ctrl->pass_dst[a.pass];
   const uint32_t* kin = src == kSelInput ? a.input : (src == kSelA ? a.keys_a : a.keys_b);
   const uint32_t* rin = src == kSelInput ? nullptr : (src == kSelA ? a.rids_a : a.rids_b);
-  uint32_t* kout = dst == kSelA ? a.keys_a : a.keys_b;
-  uint32_t* rout = dst == kSelA ? a.rids_a : a.rids_b;
+  uint32_t* __restrict__ kout = dst == kSelA ? a.keys_a : a.keys_b;
+  uint32_t* __restrict__ rout = dst == kSelA ? a.rids_a : a.rids_b;
 
-  const uint32_t tid = threadIdx.x;
+  const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint32_t shift = a.pass * kRadixBits;
+  const uint64_t lo = (uint64_t)blockIdx.x * a.g.range_rows;
+  if (lo >= a.n) return;
+  const uint64_t hi = lo + a.g.range_rows < a.n ? lo + a.g.range_rows : a.n;
+  const uint32_t ntiles = (uint32_t)ceil_div(hi - lo, TILE);
+
+  sm.run_off[tid] = a.range_start[(uint64_t)blockIdx.x * kRadix + tid];
   if (tid == 0) {
-    sm.tile = atomicAdd(&a.ctrl->tile_ctr[a.pass], 1u);
+    mbar_init(&sm.bar[0], 1);
+    mbar_init(&sm.bar[1], 1);
     sm.abort = 0;
-  }
-  {
-    uint4* w4 = reinterpret_cast<uint4*>(&sm.whist[0][0]);
-    for (uint32_t i = tid; i < kSortWarps * kRadix / 4; i += kSortThreads)
-      w4[i] = make_uint4(0, 0, 0, 0);
+    fence_mbar_init();
+    if (hi - lo >= TILE) fetch_tile(sm.in_keys[0], sm.in_rids[0], &sm.bar[0], kin, rin, lo, TILE);
   }
   __syncthreads();
-  const uint32_t tile = sm.tile;
-  onesweep_tile<ITEMS>(a, sm, kin, rin, kout, rout, tile, (uint64_t)tile * TILE);
+
+  const uint32_t row0 = warp * 32 * ITEMS + lane;  // tile row of item 0
+  const uint32_t lt = lanemask_lt(), gt = lanemask_gt();
+  uint32_t* whA = sm.whist[warp][0];
+  uint32_t* whB = sm.whist[warp][1];
+
+  for (uint32_t i = 0; i < ntiles; ++i) {
+    const uint32_t cur = i & 1;
+    const uint64_t base = lo + (uint64_t)i * TILE;
+    const uint32_t valid = hi - base < TILE ? (uint32_t)(hi - base) : TILE;
+    // Prefetch tile i + 1 into the other buffer (read during tile i - 1,
+    // whose reads ended at the barrier that closed that iteration).  Only the
+    // column's last tile can be ragged; it is read with plain loads instead.
+    if (tid == 0 && i + 1 < ntiles && hi - (base + TILE) >= TILE)
+      fetch_tile(sm.in_keys[cur ^ 1], sm.in_rids[cur ^ 1], &sm.bar[cur ^ 1], kin, rin,
+                 base + TILE, TILE);
+    // Zero the warp counters (the previous tile's last reads were fenced).
+    {
+      uint4* w4 = reinterpret_cast<uint4*>(&sm.whist[0][0][0]);
+      for (uint32_t k = tid; k < 2 * kSortWarps * kRadix / 4; k += kSortThreads)
+        w4[k] = make_uint4(0, 0, 0, 0);
+    }
+    uint32_t key[ITEMS];
+    if (valid == TILE) {
+      // i-th use of this buffer's barrier completes phase (i / 2) & 1
+      if (!mbar_wait_bounded(&sm.bar[cur], (i >> 1) & 1)) {
+        set_status(a.status, WAH_ETIMEOUT);
+        sm.abort = 1;
+      }
+      const uint32_t* kp = sm.in_keys[cur] + row0;
+#pragma unroll
+      for (int j = 0; j < ITEMS; ++j) key[j] = kp[j * 32];
+    } else {
+      // The column's ragged last tile: plain loads; rows past n get key
+      // 0xFFFFFFFF (digit 255 in every pass: stable ranking puts them after
+      // every real row of the last bin, at tile positions >= valid, which are
+      // never written out).
+#pragma unroll
+      for (int j = 0; j < ITEMS; ++j) {
+        const uint32_t r = row0 + j * 32;
+        key[j] = r < valid ? kin[base + r] : 0xffffffffu;
+        if (rin) sm.in_rids[cur][r] = r < valid ? rin[base + r] : 0u;
+      }
+    }
+    __syncthreads();
+
+    // Peer masks (independent), then two interleaved counter chains.
+    uint32_t rank[ITEMS];
+#pragma unroll
+    for (int j = 0; j < ITEMS; ++j) rank[j] = digit_peers<BALLOT>(bfe(key[j], shift, kRadixBits));
+#pragma unroll
+    for (int j = 0; j < HALF; ++j) {
+      const uint32_t pa = rank[j], pb = rank[j + HALF];
+      const uint32_t da = bfe(key[j], shift, kRadixBits);
+      const uint32_t db = bfe(key[j + HALF], shift, kRadixBits);
+      const uint32_t ca = whA[da];
+      const uint32_t cb = whB[db];
+      __syncwarp();
+      if ((pa & gt) == 0) whA[da] = ca + __popc(pa);
+      if ((pb & gt) == 0) whB[db] = cb + __popc(pb);
+      __syncwarp();
+      rank[j] = ca + __popc(pa & lt);
+      rank[j + HALF] = cb + __popc(pb & lt);
+    }
+#pragma unroll
+    for (int j = HALF; j < ITEMS; ++j) rank[j] += whA[bfe(key[j], shift, kRadixBits)];
+    __syncthreads();
+
+    // Thread b: tile count of bin b, tile-local bin start, warp starts.
+    const uint32_t b = tid;
+    uint32_t cnt[kSortWarps];
+    uint32_t count = 0;
+#pragma unroll
+    for (int w = 0; w < kSortWarps; ++w) {
+      cnt[w] = sm.whist[w][0][b] + sm.whist[w][1][b];
+      count += cnt[w];
+    }
+    uint32_t tile_total;
+    const uint32_t lstart = block_exclusive_scan<kSortThreads>(count, &tile_total, sm.warp_tmp);
+    {
+      uint32_t run = lstart;
+#pragma unroll
+      for (int w = 0; w < kSortWarps; ++w) {
+        sm.whist[w][0][b] = run;
+        run += cnt[w];
+      }
+    }
+    sm.bin_base[b] = sm.run_off[b] - lstart;
+    sm.run_off[b] += count;
+    __syncthreads();
+
+    // Stage in tile-sorted order.
+    uint32_t* out_keys = sm.in_keys[cur];
+    const uint32_t* rsrc = sm.in_rids[cur] + row0;
+    const uint32_t rid0 = (uint32_t)base + row0;
+#pragma unroll
+    for (int j = 0; j < ITEMS; ++j) {
+      const uint32_t r = whA[bfe(key[j], shift, kRadixBits)] + rank[j];
+      out_keys[r] = key[j];
+      sm.out_rids[r] = rin ? rsrc[j * 32] : rid0 + j * 32;
+    }
+    __syncthreads();
+
+    if (!sm.abort) {
+      const uint32_t n32 = (uint32_t)a.n;
+#pragma unroll 4
+      for (int it = 0; it < ITEMS; ++it) {
+        const uint32_t k = it * kSortThreads + tid;
+        if (k < valid) {
+          const uint32_t kk = out_keys[k];
+          const uint32_t g = sm.bin_base[bfe(kk, shift, kRadixBits)] + k;
+          if (g < n32) {
+            kout[g] = kk;
+            rout[g] = sm.out_rids[k];
+          } else {
+            set_status(a.status, WAH_ETIMEOUT);
+          }
+        }
+      }
+    }
+    __syncthreads();  // staging and input buffer reusable
+  }
 }
 
-// Compiled tile shapes of the onesweep pass (rows per thread, CTAs per SM the
-// register budget is fitted to).  sort_items selects one; the autotuner
-// measures them.
+// ---------------------------------------------------------------------------
+// Host side.
+// ---------------------------------------------------------------------------
+// Compiled tile shapes of the scatter pass; sort_items selects one, the
+// autotuner measures them.
 struct SortVariant {
   int items;
-  void (*fn)(SortPassArgs);
+  void (*fn)(ScatterArgs);
   size_t smem;
 };
 
-SortVariant sort_variant(int items) {
+SortVariant sort_variant(int items, bool ballot) {
+  if (ballot) {
+    switch (items) {
+      case 8: return {8, k_radix_scatter<8, true>, sizeof(ScatterSmem<8>)};
+      case 12: return {12, k_radix_scatter<12, true>, sizeof(ScatterSmem<12>)};
+      default: return {16, k_radix_scatter<16, true>, sizeof(ScatterSmem<16>)};
+    }
+  }
   switch (items) {
-    case 8: return {8, k_onesweep_pass<8, 4>, sizeof(SortPassSmem<8>)};
-    case 12: return {12, k_onesweep_pass<12, 3>, sizeof(SortPassSmem<12>)};
-    case 20: return {20, k_onesweep_pass<20, 2>, sizeof(SortPassSmem<20>)};
-    default: return {16, k_onesweep_pass<16, 2>, sizeof(SortPassSmem<16>)};
+    case 8: return {8, k_radix_scatter<8, false>, sizeof(ScatterSmem<8>)};
+    case 12: return {12, k_radix_scatter<12, false>, sizeof(ScatterSmem<12>)};
+    default: return {16, k_radix_scatter<16, false>, sizeof(ScatterSmem<16>)};
   }
 }
 
-uint64_t sort_tiles(uint64_t n, int items) {
-  return ceil_div(n, (uint64_t)kSortThreads * sort_variant(items).items);
+// Equal ranges of whole tiles, one per resident scatter CTA.
+RangeGeom range_geometry(uint64_t n, int resident_ctas, int items) {
+  const uint64_t tile = (uint64_t)kSortThreads * items;
+  uint64_t want = (uint64_t)std::max(resident_ctas, 1);
+  if (want > kMaxRanges) want = kMaxRanges;
+  RangeGeom g;
+  g.range_rows = std::max<uint64_t>(ceil_div(ceil_div(n, want), tile) * tile, tile);
+  g.ranges = (uint32_t)std::max<uint64_t>(ceil_div(n, g.range_rows), 1);
+  return g;
 }
 
 cudaError_t launch_sort(const SortLaunch& a, cudaStream_t s, uint32_t* launches) {
   const uint64_t n = a.n;
-  // Histogram: enough CTAs to keep every SM busy with 16-byte loads in flight.
-  {
-    const uint64_t work = ceil_div(n / 128 + 1, (uint64_t)kHistWarps * kHistUnroll);
-    const uint64_t cap = (uint64_t)a.sm_count * 8;
-    const int grid = (int)(work < cap ? work : cap);
-    record_phase(a.events, kPhaseHist, false, s);
-    switch (a.passes) {
-      case 1: k_digit_histogram<1><<<grid, kHistThreads, 0, s>>>(a.values, n, a.ctrl); break;
-      case 2: k_digit_histogram<2><<<grid, kHistThreads, 0, s>>>(a.values, n, a.ctrl); break;
-      case 3: k_digit_histogram<3><<<grid, kHistThreads, 0, s>>>(a.values, n, a.ctrl); break;
-      default: k_digit_histogram<4><<<grid, kHistThreads, 0, s>>>(a.values, n, a.ctrl); break;
-    }
-    record_phase(a.events, kPhaseHist, true, s);
-    ++*launches;
+  const SortVariant v = sort_variant(a.sort_items, a.sort_ballot);
+  cudaError_t err =
+      cudaFuncSetAttribute(v.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)v.smem);
+  if (err != cudaSuccess) return err;
+  int per_sm = 0;
+  err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, v.fn, kSortThreads, v.smem);
+  if (err != cudaSuccess) return err;
+  const RangeGeom g = range_geometry(n, a.sm_count * std::max(per_sm, 1), v.items);
+  const unsigned count_grid = g.ranges * kCountCtasPerRange;
+  err = cudaMemsetAsync(a.range_hist, 0, (size_t)kDigits * kMaxRanges * kRadix * 4, s);
+  if (err != cudaSuccess) return err;
+
+  record_phase(a.events, kPhaseHist, false, s);
+  switch (a.passes) {
+    case 1:
+      k_digit_histogram<1><<<count_grid, kHistThreads, 0, s>>>(a.values, n, g, a.ctrl,
+                                                               a.range_hist);
+      break;
+    case 2:
+      k_digit_histogram<2><<<count_grid, kHistThreads, 0, s>>>(a.values, n, g, a.ctrl,
+                                                               a.range_hist);
+      break;
+    case 3:
+      k_digit_histogram<3><<<count_grid, kHistThreads, 0, s>>>(a.values, n, g, a.ctrl,
+                                                               a.range_hist);
+      break;
+    default:
+      k_digit_histogram<4><<<count_grid, kHistThreads, 0, s>>>(a.values, n, g, a.ctrl,
+                                                               a.range_hist);
+      break;
   }
+  record_phase(a.events, kPhaseHist, true, s);
+  ++*launches;
   record_phase(a.events, kPhasePlan, false, s);
   k_sort_plan<<<1, kRadix, 0, s>>>(a.ctrl, n, a.passes, a.status);
   record_phase(a.events, kPhasePlan, true, s);
   ++*launches;
-  cudaError_t err = cudaGetLastError();
+  err = cudaGetLastError();
   if (err != cudaSuccess) return err;
 
-  SortPassArgs pa;
-  pa.input = a.values;
-  pa.keys_a = a.buf_keys[0];
-  pa.rids_a = a.buf_rids[0];
-  pa.keys_b = a.buf_keys[1];
-  pa.rids_b = a.buf_rids[1];
-  pa.n = n;
-  pa.ctrl = a.ctrl;
-  pa.lookback = a.lb_sort;
-  pa.status = a.status;
-  const SortVariant v = sort_variant(a.sort_items);
-  const uint64_t tiles = ceil_div(n, (uint64_t)kSortThreads * v.items);
-  err = cudaFuncSetAttribute(v.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)v.smem);
-  if (err != cudaSuccess) return err;
+  ScatterArgs sa;
+  sa.input = a.values;
+  sa.keys_a = a.buf_keys[0];
+  sa.rids_a = a.buf_rids[0];
+  sa.keys_b = a.buf_keys[1];
+  sa.rids_b = a.buf_rids[1];
+  sa.n = n;
+  sa.g = g;
+  sa.ctrl = a.ctrl;
+  sa.range_start = a.range_start;
+  sa.status = a.status;
   for (int p = 0; p < kDigits; ++p) {
     if (p >= a.passes) {  // not launched: empty span keeps every event valid
       record_phase(a.events, kPhasePass0 + p, false, s);
       record_phase(a.events, kPhasePass0 + p, true, s);
       continue;
     }
-    err = cudaMemsetAsync(a.lb_sort, 0, tiles * kRadix * sizeof(uint32_t), s);
-    if (err != cudaSuccess) return err;
-    pa.pass = p;
+    uint32_t* rh = a.range_hist + (size_t)p * kMaxRanges * kRadix;
     record_phase(a.events, kPhasePass0 + p, false, s);
-    v.fn<<<(unsigned)tiles, kSortThreads, v.smem, s>>>(pa);
-    record_phase(a.events, kPhasePass0 + p, true, s);
+    if (p > 0) {
+      k_range_count<<<count_grid, kHistThreads, 0, s>>>(a.values, a.buf_keys[0], a.buf_keys[1],
+                                                        n, g, p, a.ctrl, rh);
+      ++*launches;
+    }
+    k_range_scan<<<1, kRadix, 0, s>>>(a.ctrl, p, g.ranges, rh, a.range_start);
     ++*launches;
+    sa.pass = p;
+    v.fn<<<g.ranges, kSortThreads, v.smem, s>>>(sa);
+    ++*launches;
+    record_phase(a.events, kPhasePass0 + p, true, s);
     err = cudaGetLastError();
     if (err != cudaSuccess) return err;
   }
