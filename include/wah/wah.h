@@ -93,6 +93,24 @@ int wah_build(const uint32_t* d_values, uint64_t n, uint32_t bound,
               void* stream);
 
 /*
+ * wah_build for callers that cannot allocate device memory (no counterpart in
+ * the reference).  An ingest plugin whose host engine owns the device memory
+ * pool, or a serving loop that cannot afford the device synchronisation of
+ * cudaMalloc/cudaFree, passes only the column and the output buffers; the
+ * build's scratch memory is a fixed array in the library's device image
+ * (22 MiB, held by every GPU that loads the library until exit).  Columns of
+ * up to WAH_NOALLOC_MAX_ROWS rows; larger n returns WAH_ERANGE without
+ * enqueueing anything.  Calls no allocator.  All calls share the array:
+ * calls whose work overlaps on the GPU (unordered streams or host threads)
+ * race.  The first call on a device looks up the array's device address with
+ * that device current; make it before any stream capture on the device.
+ */
+#define WAH_NOALLOC_MAX_ROWS ((uint64_t)1 << 20)
+int wah_build_noalloc(const uint32_t* d_values, uint64_t n, uint32_t bound,
+                      uint32_t* d_keys, uint32_t* d_offsets, uint32_t* d_index,
+                      wah_counts* d_counts, void* stream);
+
+/*
  * Phase a1 alone: stable sort of d_values by value carrying row ids
  * (src/cpu.cpp:180-197 semantics; src/phases.cpp:730-773 on the GPU).
  * Writes d_sorted_values[n] and d_rids[n].  Same bound and workspace rules as

@@ -19,7 +19,7 @@ INCLUDE = os.path.join(REPO_DIR, "include")
 OBJ_DIR = os.path.join(PKG_DIR, "_build")
 LIB_PATH = os.path.join(PKG_DIR, "libwah_gb300.so")
 
-CUDA_SOURCES = ["wah_sort.cu", "wah_index.cu", "wah_api.cu"]
+CUDA_SOURCES = ["wah_sort.cu", "wah_index.cu", "wah_api.cu", "wah_noalloc.cu"]
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo",
               "-std=c++17", "-Xcompiler", "-fPIC", "-I" + INCLUDE, "-I" + CSRC]
 
@@ -74,6 +74,7 @@ SIGNATURES = {
     "wah_workspace_bytes": ([_u64, _u32], ctypes.c_size_t),
     "wah_build": ([_vp, _u64, _u32, _vp, _vp, _vp, _vp, _vp, ctypes.c_size_t, _vp],
                   ctypes.c_int),
+    "wah_build_noalloc": ([_vp, _u64, _u32, _vp, _vp, _vp, _vp, _vp], ctypes.c_int),
     "wah_sort_rids_by_value": ([_vp, _u64, _u32, _vp, _vp, _vp, _vp, ctypes.c_size_t, _vp],
                                ctypes.c_int),
     "wah_build_sorted": ([_vp, _vp, _u64, _vp, _vp, _vp, _vp, _vp, ctypes.c_size_t, _vp],
