@@ -34,7 +34,7 @@ WsLayout ws_layout(uint64_t n) {
   l.range_start = off;
   off += align_up((size_t)kMaxRanges * kRadix * sizeof(uint32_t));
   l.lb_build = off;
-  off += align_up(ceil_div(std::max<uint64_t>(n, 1), kBuildTile) * sizeof(uint64_t));
+  off += align_up((size_t)kMaxRanges * 6 * sizeof(uint32_t));
   const size_t col = align_up(std::max<uint64_t>(n, 1) * sizeof(uint32_t));
   l.keys_a = off;
   off += col;
@@ -182,7 +182,9 @@ static int build_impl(const uint32_t* d_values, uint64_t n, uint32_t bound, uint
   b.sel = -1;
   b.n = n;
   b.ctrl = reinterpret_cast<WahCtrl*>(ws + l.ctrl);
-  b.lb_build = reinterpret_cast<uint64_t*>(ws + l.lb_build);
+  b.range_counts = reinterpret_cast<uint32_t*>(ws + l.lb_build);
+  b.range_first = b.range_counts + kMaxRanges * 4;
+  b.sm_count = sm_count_current();
   b.keys = d_keys;
   b.offsets = d_offsets;
   b.index = d_index;
@@ -284,7 +286,9 @@ int wah_build_sorted(const uint32_t* d_sorted_values, const uint32_t* d_rids, ui
   b.sel = 0;
   b.n = n;
   b.ctrl = ctrl;
-  b.lb_build = reinterpret_cast<uint64_t*>(ws + l.lb_build);
+  b.range_counts = reinterpret_cast<uint32_t*>(ws + l.lb_build);
+  b.range_first = b.range_counts + kMaxRanges * 4;
+  b.sm_count = sm_count_current();
   b.keys = d_keys;
   b.offsets = d_offsets;
   b.index = d_index;

@@ -168,13 +168,16 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
-// Bounded wait for a phase of an mbarrier; false after kSpinLimit polls.
+// Bounded wait for a phase of an mbarrier: false after about kWaitCycles SM
+// clocks (~1 s).  try_wait may itself suspend for a while, so the bound is on
+// elapsed clocks, not on polls.
+constexpr long long kWaitCycles = 2000000000ll;
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
-  for (uint32_t i = 0; i < kSpinLimit; ++i) {
-    if (mbar_try_wait(bar, parity)) return true;
-    if (i > kSpinFast) __nanosleep(64);
+  const long long t0 = clock64();
+  while (!mbar_try_wait(bar, parity)) {
+    if (clock64() - t0 > kWaitCycles) return false;
   }
-  return false;
+  return true;
 }
 
 // First error wins.
@@ -285,7 +288,9 @@ struct BuildLaunch {
   int sel;  // -1: take WahCtrl::final_sel, else a fixed selector
   uint64_t n;
   WahCtrl* ctrl;
-  uint64_t* lb_build;  // tiles u64
+  uint32_t* range_counts;  // [kMaxRanges][4] words, keys, segments per range
+  uint32_t* range_first;   // [kMaxRanges][2] first word and key of each range
+  int sm_count;
   uint32_t* keys;
   uint32_t* offsets;
   uint32_t* index;

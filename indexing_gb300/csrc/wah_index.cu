@@ -1,5 +1,4 @@
-// wah_index.cu -- phases a2..a6 fused into one pass over the sorted
-// (value, rid) stream.
+// wah_index.cu -- phases a2..a6 fused over the sorted (value, rid) stream.
 //
 // Reference steps (sequential semantics, src/cpu.cpp):
 //   produce_chunk_id_literals  chid = rid / 31, lit = 1<<31 | 1<<(rid % 31)
@@ -14,292 +13,427 @@
 // The reference GPU path runs these as ~20 kernels with three stream
 // compactions and host read-backs of k (src/phases.cpp:817-1077).
 //
-// Here one kernel does all of it, over tiles of 2048 sorted rows (256
-// threads x 8 consecutive rows, loaded with 128-bit loads into registers and
-// mirrored in shared memory with one row of look-behind and 30 rows of
-// look-ahead: a (value, chunk) segment has at most 31 rows, so the tile that
-// owns a segment's head can finish its literal).  Each row is classified
-// locally: segment head when (value, chunk) changes, value head when the
-// value changes; a head emits 1 + (fill != 0) words.  Literals come from a
-// reverse segmented OR over the thread's rows.  One packed block scan plus a
-// decoupled look-back across tiles (64-bit entries carrying the word and key
-// prefixes together) gives every head its final position; words, keys and
-// offsets are staged in shared memory and written once, coalesced, with no
-// zero words and no compaction pass.
+// Every row is classified from itself and the row before it: head of a
+// (value, chunk) segment when either changes, head of a value when the value
+// changes; a head emits 1 + (fill != 0) words.  The sorted stream is cut into
+// equal row ranges, one per resident emit CTA:
+//   k_build_count  streams the range's rows (128-bit loads) and counts its
+//                  words, keys and segments
+//   k_build_scan   exclusive scan over ranges: each range's first word and key
+//   k_build_emit   one persistent CTA per range walks its tiles of 2048 rows;
+//                  the next tile's window (4 rows behind, 32 ahead: a segment
+//                  has at most 31 rows, so the tile owning a segment's head
+//                  can finish its literal) is fetched by cp.async.bulk while
+//                  this one is processed; literals come from a reverse
+//                  segmented OR over each thread's 8 rows; a block scan gives
+//                  tile-local positions; words, keys and offsets are staged in
+//                  shared memory and written once, coalesced, at the range's
+//                  running offsets.  No zero word is ever written and no
+//                  compaction pass is needed.
+#include <algorithm>
+
 #include "wah_common.cuh"
 
 namespace wah {
 
-constexpr int kLookAhead = 30;  // a segment has at most 31 rows
-constexpr int kWinRows = kBuildTile + kLookAhead + 2;
+constexpr int kLookAhead = 30;  // rows after a tile that can continue its last segment
+constexpr int kWinBehind = 4;   // window starts 4 rows before the tile (16-byte aligned)
+constexpr int kWinRows = kWinBehind + kBuildTile + 32;  // rows fetched per tile
 
 // Staging index skew: position i lives at i + i/16, so threads writing runs
 // that start ~16 words apart hit different banks.
 __device__ __forceinline__ uint32_t skew(uint32_t i) { return i + (i >> 4); }
 constexpr int kSkewed(int n) { return n + n / 16 + 1; }
 
-struct BuildSmem {
-  uint32_t v[kWinRows];   // sorted values of rows base .. base+TILE+29
-  uint32_t cb[kWinRows];  // (chunk << 5) | (rid % 31) of the same rows
-  uint32_t words[kSkewed(2 * kBuildTile)];
-  uint32_t keys[kSkewed(kBuildTile)];
-  uint32_t offs[kSkewed(kBuildTile)];
-  uint64_t warp_tmp[kBuildThreads / 32 + 1];
-  uint64_t tile_prefix;  // exclusive (keys << 32 | words) before this tile
-  uint32_t prev_v, prev_cb;
-  uint32_t tile;
-  int abort;
-};
-
 __device__ __forceinline__ uint32_t chunk_bit(uint32_t rid) {
   const uint32_t c = rid / 31;
   return (c << 5) | (rid - c * 31);
 }
 
-// Look-back over earlier tiles by warp 0; returns the exclusive prefix.
-__device__ __forceinline__ uint64_t build_lookback(uint64_t* __restrict__ lb, uint32_t tile,
-                                                   uint32_t* status, int* abort) {
-  const int lane = threadIdx.x & 31;
-  uint64_t excl = 0;
-  int64_t k = (int64_t)tile - 1 - lane;
-  uint32_t spins = 0;
-  while (true) {
-    const uint64_t e = k >= 0 ? ld_relaxed_u64(lb + k) : kLbPrefix64;
-    const uint32_t fl = (uint32_t)(e >> 62);
-    if (__any_sync(0xffffffffu, fl == 0)) {
-      if (++spins > kSpinLimit) {
-        if (lane == 0) {
-          set_status(status, WAH_ETIMEOUT);
-          *abort = 1;
-        }
-        break;
-      }
-      __nanosleep(spins > kSpinFast ? 256 : 32);
-      continue;
-    }
-    const uint32_t pmask = __ballot_sync(0xffffffffu, fl == 2);
-    const int stop = pmask ? __ffs(pmask) - 1 : 31;
-    uint64_t val = lane <= stop ? (e & kLbMask64) : 0;
-#pragma unroll
-    for (int d = 16; d > 0; d >>= 1) val += __shfl_xor_sync(0xffffffffu, val, d);
-    excl += val;
-    if (pmask) break;
-    k -= 32;
-  }
-  return excl;
-}
-
-// Per-thread counters packed for one block scan: words | keys << 21 | segs << 42.
+// Per-thread counters packed for one block scan: words | keys << 21.
 constexpr int kPackShift = 21;
 constexpr uint64_t kPackMask = (1ull << kPackShift) - 1;
 
-__global__ void __launch_bounds__(kBuildThreads, 4)
-    k_wah_build(SortBufs bufs, int sel, uint64_t n, WahCtrl* ctrl, uint64_t* __restrict__ lb,
-                uint32_t* __restrict__ keys, uint32_t* __restrict__ offsets,
-                uint32_t* __restrict__ index, uint64_t keys_cap, uint64_t index_cap,
-                wah_counts* counts) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  BuildSmem& sm = *reinterpret_cast<BuildSmem*>(smem_raw);
-  uint32_t* status = &counts->status;
+// ---------------------------------------------------------------------------
+// Count: words, keys, segments per range.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void count_row(uint32_t v, uint32_t c, uint32_t pv, uint32_t pc,
+                                          uint32_t& words, uint32_t& keys, uint32_t& segs) {
+  const bool vh = v != pv;
+  const bool h = vh || c != pc;
+  const uint32_t fill = vh ? c : c - pc - 1;
+  words += h ? 1u + (fill != 0) : 0u;
+  keys += vh;
+  segs += h;
+}
 
+__global__ void __launch_bounds__(kHistThreads)
+    k_build_count(SortBufs bufs, int sel, uint64_t n, RangeGeom g, const WahCtrl* ctrl,
+                  uint32_t* __restrict__ range_counts /* [ranges][4] */) {
   const int s = sel >= 0 ? sel : ctrl->final_sel;
   const uint32_t* __restrict__ sv = s == 0 ? bufs.keys[0] : (s == 1 ? bufs.keys[1] : bufs.keys[2]);
   const uint32_t* __restrict__ sr = s == 0 ? bufs.rids[0] : (s == 1 ? bufs.rids[1] : bufs.rids[2]);
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t c = blockIdx.x / kCountCtasPerRange, q = blockIdx.x % kCountCtasPerRange;
+  const uint64_t part = g.range_rows / kCountCtasPerRange;  // multiple of 4
+  uint64_t lo = (uint64_t)c * g.range_rows + q * part;
+  uint64_t hi = q + 1 == kCountCtasPerRange ? (uint64_t)(c + 1) * g.range_rows : lo + part;
+  lo = lo < n ? lo : n;
+  hi = hi < n ? hi : n;
 
-  const uint32_t tid = threadIdx.x;
-  if (tid == 0) {
-    sm.tile = atomicAdd(&ctrl->tile_ctr[4], 1u);
-    sm.abort = 0;
-  }
-  __syncthreads();
-  const uint32_t tile = sm.tile;
-  const uint64_t base = (uint64_t)tile * kBuildTile;
-  const bool full = base + kBuildTile <= n;
-  const uint32_t valid = full ? kBuildTile : (uint32_t)(n - base);
-  // rows of the window that exist (tile + look-ahead, clipped at n)
-  const uint64_t left = n - base;
-  const uint32_t wend = left < (uint64_t)(kBuildTile + kLookAhead) ? (uint32_t)left
-                                                                    : (uint32_t)(kBuildTile + kLookAhead);
-
-  // This thread's rows: first .. first+7 of the tile, in registers.
-  const uint32_t first = tid * kBuildItems;
-  uint32_t v[kBuildItems], cb[kBuildItems];
-  if (full) {
-    const uint4* v4 = reinterpret_cast<const uint4*>(sv + base + first);
-    const uint4 a0 = v4[0], a1 = v4[1];
-    v[0] = a0.x; v[1] = a0.y; v[2] = a0.z; v[3] = a0.w;
-    v[4] = a1.x; v[5] = a1.y; v[6] = a1.z; v[7] = a1.w;
+  uint32_t words = 0, keys = 0, segs = 0;
+  const uint64_t chunks = (hi - lo) / 128;  // 32 lanes x 4 rows
+  for (uint64_t k = warp; k < chunks; k += kHistWarps) {
+    const uint64_t p = lo + k * 128 + lane * 4;
+    const uint4 v4 = ld_stream_v4(reinterpret_cast<const uint4*>(sv + p));
+    uint4 r4;
     if (sr) {
-      const uint4* r4 = reinterpret_cast<const uint4*>(sr + base + first);
-      const uint4 b0 = r4[0], b1 = r4[1];
-      cb[0] = chunk_bit(b0.x); cb[1] = chunk_bit(b0.y); cb[2] = chunk_bit(b0.z);
-      cb[3] = chunk_bit(b0.w); cb[4] = chunk_bit(b1.x); cb[5] = chunk_bit(b1.y);
-      cb[6] = chunk_bit(b1.z); cb[7] = chunk_bit(b1.w);
+      r4 = ld_stream_v4(reinterpret_cast<const uint4*>(sr + p));
     } else {
-#pragma unroll
-      for (int j = 0; j < kBuildItems; ++j) cb[j] = chunk_bit((uint32_t)base + first + j);
+      r4 = make_uint4((uint32_t)p, (uint32_t)p + 1, (uint32_t)p + 2, (uint32_t)p + 3);
     }
-  } else {
-#pragma unroll
-    for (int j = 0; j < kBuildItems; ++j) {
-      const bool ok = first + j < valid;
-      v[j] = ok ? sv[base + first + j] : 0u;
-      const uint32_t r = ok ? (sr ? sr[base + first + j] : (uint32_t)base + first + j) : 0u;
-      cb[j] = chunk_bit(r);
-    }
-  }
-  {
-    uint4* wv = reinterpret_cast<uint4*>(&sm.v[first]);
-    uint4* wc = reinterpret_cast<uint4*>(&sm.cb[first]);
-    wv[0] = make_uint4(v[0], v[1], v[2], v[3]);
-    wv[1] = make_uint4(v[4], v[5], v[6], v[7]);
-    wc[0] = make_uint4(cb[0], cb[1], cb[2], cb[3]);
-    wc[1] = make_uint4(cb[4], cb[5], cb[6], cb[7]);
-  }
-  // Look-ahead rows (segments that start in this tile end inside them).
-  if (tid < kLookAhead) {
-    const uint32_t i = kBuildTile + tid;
-    if (i < wend) {
-      sm.v[i] = sv[base + i];
-      sm.cb[i] = chunk_bit(sr ? sr[base + i] : (uint32_t)(base + i));
-    }
-  }
-  // Look-behind row: the last row of the previous tile, or, for the first
-  // tile, a value that differs from row 0 (so row 0 heads a new key).
-  if (tid == kBuildThreads - 1) {
-    if (base > 0) {
-      sm.prev_v = sv[base - 1];
-      sm.prev_cb = chunk_bit(sr ? sr[base - 1] : (uint32_t)(base - 1));
-    } else {
-      sm.prev_v = ~sv[0];
-      sm.prev_cb = 0;
-    }
-  }
-  __syncthreads();
-
-  // Classify rows: head of a (value, chunk) segment / head of a value.
-  uint32_t pv = tid ? sm.v[first - 1] : sm.prev_v;
-  uint32_t pc = (tid ? sm.cb[first - 1] : sm.prev_cb) >> 5;
-  uint32_t headm = 0, vheadm = 0, fills[kBuildItems];
-  uint32_t nw = 0;
-#pragma unroll
-  for (int j = 0; j < kBuildItems; ++j) {
-    const uint32_t c = cb[j] >> 5;
-    const bool ok = full || first + j < valid;
-    const bool vh = v[j] != pv;
-    const bool h = ok && (vh || c != pc);
-    fills[j] = vh ? c : c - pc - 1;
-    if (h) {
-      headm |= 1u << j;
-      if (vh) vheadm |= 1u << j;
-      nw += 1 + (fills[j] != 0);
-    }
-    pv = v[j];
-    pc = c;
-  }
-  const uint32_t nk = __popc(vheadm), ns = __popc(headm);
-
-  // Literals: reverse segmented OR.  First the rows after this thread's last
-  // row that continue its last segment (from shared memory), then backwards.
-  uint32_t acc = 0;
-  {
-    const uint32_t c7 = cb[kBuildItems - 1] >> 5;
-    for (uint32_t m = first + kBuildItems; m < wend; ++m) {
-      if (sm.v[m] != v[kBuildItems - 1] || (sm.cb[m] >> 5) != c7) break;
-      acc |= 1u << (sm.cb[m] & 31);
-    }
-  }
-  uint32_t lits[kBuildItems];
-#pragma unroll
-  for (int j = kBuildItems - 1; j >= 0; --j) {
-    if (full || first + j < valid) acc |= 1u << (cb[j] & 31);  // rows past n add nothing
-    lits[j] = acc | 0x80000000u;
-    if (headm & (1u << j)) acc = 0;
-  }
-
-  uint64_t tile_agg;
-  const uint64_t my_prefix = block_exclusive_scan64<kBuildThreads>(
-      (uint64_t)nw | ((uint64_t)nk << kPackShift) | ((uint64_t)ns << (2 * kPackShift)), &tile_agg,
-      sm.warp_tmp);
-  const uint32_t tw = (uint32_t)(tile_agg & kPackMask);
-  const uint32_t tk = (uint32_t)((tile_agg >> kPackShift) & kPackMask);
-  const uint32_t ts = (uint32_t)(tile_agg >> (2 * kPackShift));
-
-  if (tid == 0 && ts) atomicAdd(&counts->merged, ts);
-  const uint64_t agg = ((uint64_t)tk << 32) | tw;
-  if (tid == 0) st_relaxed_u64(lb + tile, (tile == 0 ? kLbPrefix64 : kLbAggregate64) | agg);
-
-  // Stage this thread's words, keys and offsets at tile-local positions
-  // (before the look-back, which then finds its predecessors published).
-  uint32_t pw = (uint32_t)(my_prefix & kPackMask);
-  uint32_t pk = (uint32_t)((my_prefix >> kPackShift) & kPackMask);
-#pragma unroll
-  for (int j = 0; j < kBuildItems; ++j) {
-    if (headm & (1u << j)) {
-      if (vheadm & (1u << j)) {
-        sm.keys[skew(pk)] = v[j];
-        sm.offs[skew(pk)] = pw;  // tile-local; the tile's word prefix is added below
-        ++pk;
+    // row p - 1: the previous lane's last row, or a load for lane 0
+    uint32_t pv = __shfl_up_sync(0xffffffffu, v4.w, 1);
+    uint32_t pr = __shfl_up_sync(0xffffffffu, r4.w, 1);
+    if (lane == 0) {
+      if (p > 0) {
+        pv = sv[p - 1];
+        pr = sr ? sr[p - 1] : (uint32_t)(p - 1);
+      } else {
+        pv = ~v4.x;  // row 0 heads a key
+        pr = 0;
       }
-      if (fills[j]) sm.words[skew(pw++)] = fills[j];
-      sm.words[skew(pw++)] = lits[j];
+    }
+    const uint32_t pc = pr / 31;
+    const uint32_t c0 = r4.x / 31, c1 = r4.y / 31, c2 = r4.z / 31, c3 = r4.w / 31;
+    count_row(v4.x, c0, pv, pc, words, keys, segs);
+    count_row(v4.y, c1, v4.x, c0, words, keys, segs);
+    count_row(v4.z, c2, v4.y, c1, words, keys, segs);
+    count_row(v4.w, c3, v4.z, c2, words, keys, segs);
+  }
+  if (warp == 0) {  // ragged end of the sub-range, one row per lane
+    for (uint64_t p = lo + chunks * 128 + lane; p < hi; p += 32) {
+      const uint32_t v = sv[p];
+      const uint32_t cc = (sr ? sr[p] : (uint32_t)p) / 31;
+      uint32_t pv, pc;
+      if (p > 0) {
+        pv = sv[p - 1];
+        pc = (sr ? sr[p - 1] : (uint32_t)(p - 1)) / 31;
+      } else {
+        pv = ~v;
+        pc = 0;
+      }
+      count_row(v, cc, pv, pc, words, keys, segs);
     }
   }
-  if (tid < 32) {
-    uint64_t excl = 0;
-    if (tile > 0) {
-      excl = build_lookback(lb, tile, status, &sm.abort);
-      if (tid == 0) st_relaxed_u64(lb + tile, kLbPrefix64 | (excl + agg));
-    }
-    if (tid == 0) sm.tile_prefix = excl;
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) {
+    words += __shfl_xor_sync(0xffffffffu, words, d);
+    keys += __shfl_xor_sync(0xffffffffu, keys, d);
+    segs += __shfl_xor_sync(0xffffffffu, segs, d);
   }
-  __syncthreads();
-  if (sm.abort) return;
-  const uint64_t tile_prefix = sm.tile_prefix;
-  const uint32_t xw = (uint32_t)(tile_prefix & 0xffffffffu);
-  const uint32_t xk = (uint32_t)(tile_prefix >> 32);
-
-  bool overflow = false;
-  for (uint32_t i = tid; i < tw; i += kBuildThreads) {
-    const uint64_t pos = (uint64_t)xw + i;
-    if (pos < index_cap)
-      index[pos] = sm.words[skew(i)];
-    else
-      overflow = true;
-  }
-  for (uint32_t i = tid; i < tk; i += kBuildThreads) {
-    const uint64_t pos = (uint64_t)xk + i;
-    if (pos < keys_cap) {
-      keys[pos] = sm.keys[skew(i)];
-      offsets[pos] = xw + sm.offs[skew(i)];
-    } else {
-      overflow = true;
-    }
-  }
-  if (overflow) set_status(status, WAH_EOVERFLOW);
-
-  // The last tile knows the totals.
-  if (tid == 0 && base + kBuildTile >= n) {
-    const uint64_t tot = tile_prefix + (((uint64_t)tk << 32) | tw);
-    counts->index_len = (uint32_t)(tot & 0xffffffffu);
-    counts->keycnt = (uint32_t)(tot >> 32);
+  if (lane == 0) {
+    if (words) atomicAdd(&range_counts[c * 4 + 0], words);
+    if (keys) atomicAdd(&range_counts[c * 4 + 1], keys);
+    if (segs) atomicAdd(&range_counts[c * 4 + 2], segs);
   }
 }
 
+// Exclusive scan of (words, keys) over ranges; totals into the counts.
+constexpr int kBuildScanThreads = 1024;
+static_assert(kBuildScanThreads >= kMaxRanges, "one thread per range");
+
+__global__ void __launch_bounds__(kBuildScanThreads)
+    k_build_scan(uint32_t ranges, const uint32_t* __restrict__ range_counts,
+                 uint32_t* __restrict__ range_first /* [ranges][2] */, wah_counts* counts) {
+  __shared__ uint64_t s_warp[kBuildScanThreads / 32 + 1];
+  const uint32_t c = threadIdx.x;
+  uint64_t x = 0;
+  uint32_t segs = 0;
+  if (c < ranges) {
+    x = ((uint64_t)range_counts[c * 4 + 1] << 32) | range_counts[c * 4 + 0];
+    segs = range_counts[c * 4 + 2];
+  }
+  uint64_t total;
+  const uint64_t excl = block_exclusive_scan64<kBuildScanThreads>(x, &total, s_warp);
+  if (c < ranges) {
+    range_first[c * 2 + 0] = (uint32_t)(excl & 0xffffffffu);
+    range_first[c * 2 + 1] = (uint32_t)(excl >> 32);
+  }
+  if (segs) atomicAdd(&counts->merged, segs);
+  if (c == 0) {
+    counts->index_len = (uint32_t)(total & 0xffffffffu);
+    counts->keycnt = (uint32_t)(total >> 32);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Emit.
+// ---------------------------------------------------------------------------
+struct EmitSmem {
+  uint32_t win_v[2][kWinRows];  // window rows base-4 .. base+TILE+31
+  uint32_t win_r[2][kWinRows];
+  uint32_t words[kSkewed(2 * kBuildTile)];
+  uint32_t keys[kSkewed(kBuildTile)];
+  uint32_t offs[kSkewed(kBuildTile)];
+  uint64_t warp_tmp[kBuildThreads / 32 + 1];
+  uint64_t bar[2];
+  int abort;
+};
+
+struct EmitArgs {
+  SortBufs bufs;
+  int sel;
+  uint64_t n;
+  RangeGeom g;
+  const WahCtrl* ctrl;
+  const uint32_t* range_first;
+  uint32_t* keys;
+  uint32_t* offsets;
+  uint32_t* index;
+  uint64_t keys_cap;
+  uint64_t index_cap;
+  uint32_t* status;
+};
+
+// A tile's window can come by bulk copy when all its rows exist and it does
+// not start before row 0.
+__device__ __forceinline__ bool window_bulk(uint64_t base, uint64_t n) {
+  return base >= (uint64_t)kWinBehind && base + kBuildTile + 32 <= n;
+}
+
+__device__ __forceinline__ void fetch_window(uint32_t* wv, uint32_t* wr, uint64_t* bar,
+                                             const uint32_t* sv, const uint32_t* sr,
+                                             uint64_t base) {
+  const uint32_t bytes = kWinRows * 4u;
+  fence_proxy_async_shared();
+  mbar_arrive_expect_tx(bar, sr ? 2 * bytes : bytes);
+  bulk_copy_g2s(wv, sv + base - kWinBehind, bytes, bar);
+  if (sr) bulk_copy_g2s(wr, sr + base - kWinBehind, bytes, bar);
+}
+
+__global__ void __launch_bounds__(kBuildThreads, 3) k_build_emit(EmitArgs a) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  EmitSmem& sm = *reinterpret_cast<EmitSmem*>(smem_raw);
+  const int s = a.sel >= 0 ? a.sel : a.ctrl->final_sel;
+  const uint32_t* __restrict__ sv =
+      s == 0 ? a.bufs.keys[0] : (s == 1 ? a.bufs.keys[1] : a.bufs.keys[2]);
+  const uint32_t* __restrict__ sr =
+      s == 0 ? a.bufs.rids[0] : (s == 1 ? a.bufs.rids[1] : a.bufs.rids[2]);
+
+  const uint32_t tid = threadIdx.x;
+  const uint64_t n = a.n;
+  const uint64_t lo = (uint64_t)blockIdx.x * a.g.range_rows;
+  if (lo >= n) return;
+  const uint64_t hi = lo + a.g.range_rows < n ? lo + a.g.range_rows : n;
+  const uint32_t ntiles = (uint32_t)ceil_div(hi - lo, kBuildTile);
+  uint32_t run_w = a.range_first[blockIdx.x * 2 + 0];  // words before this tile
+  uint32_t run_k = a.range_first[blockIdx.x * 2 + 1];  // keys before this tile
+
+  if (tid == 0) {
+    mbar_init(&sm.bar[0], 1);
+    mbar_init(&sm.bar[1], 1);
+    sm.abort = 0;
+    fence_mbar_init();
+    if (window_bulk(lo, n)) fetch_window(sm.win_v[0], sm.win_r[0], &sm.bar[0], sv, sr, lo);
+  }
+  __syncthreads();
+
+  const uint32_t first = tid * kBuildItems;  // this thread's first tile row
+  uint32_t phase_bits = 0;  // parity of the next phase of bar[0], bar[1]
+  for (uint32_t i = 0; i < ntiles; ++i) {
+    const uint32_t cur = i & 1;
+    const uint64_t base = lo + (uint64_t)i * kBuildTile;
+    const uint32_t valid = hi - base < kBuildTile ? (uint32_t)(hi - base) : kBuildTile;
+    if (tid == 0 && i + 1 < ntiles && window_bulk(base + kBuildTile, n))
+      fetch_window(sm.win_v[cur ^ 1], sm.win_r[cur ^ 1], &sm.bar[cur ^ 1], sv, sr,
+                   base + kBuildTile);
+    uint32_t* wv = sm.win_v[cur];
+    uint32_t* wr = sm.win_r[cur];
+    // rows of the window that exist, counted from the tile start
+    const uint64_t left = n - base;
+    const uint32_t wend = left < (uint64_t)(kBuildTile + kLookAhead)
+                              ? (uint32_t)left
+                              : (uint32_t)(kBuildTile + kLookAhead);
+    if (window_bulk(base, n)) {
+      // phases of each buffer's barrier complete in turn; the parity of the
+      // next one is tracked per buffer (a tile read with plain loads uses none)
+      const bool ok = mbar_wait_bounded(&sm.bar[cur], (phase_bits >> cur) & 1u);
+      phase_bits ^= 1u << cur;
+      if (!ok) {
+        set_status(a.status, WAH_ETIMEOUT);
+        sm.abort = 1;
+      }
+      if (!sr) {  // identity row ids: the bulk copy brought values only
+        for (uint32_t w = tid; w < kWinRows; w += kBuildThreads)
+          wr[w] = (uint32_t)(base - kWinBehind + w);
+        __syncthreads();
+      }
+    } else {
+      // First or last tiles of the column: plain loads of the rows that exist.
+      for (uint32_t w = tid; w < kWinRows; w += kBuildThreads) {
+        const uint64_t row = base - kWinBehind + w;  // wraps below row 0: excluded
+        if (row < n) {
+          wv[w] = sv[row];
+          wr[w] = sr ? sr[row] : (uint32_t)row;
+        }
+      }
+      __syncthreads();
+    }
+
+    // This thread's 8 rows from the window (two 16-byte loads per array).
+    uint32_t v[kBuildItems], cb[kBuildItems];
+    {
+      const uint4* v4 = reinterpret_cast<const uint4*>(wv + kWinBehind + first);
+      const uint4* r4 = reinterpret_cast<const uint4*>(wr + kWinBehind + first);
+      const uint4 a0 = v4[0], a1 = v4[1], b0 = r4[0], b1 = r4[1];
+      v[0] = a0.x; v[1] = a0.y; v[2] = a0.z; v[3] = a0.w;
+      v[4] = a1.x; v[5] = a1.y; v[6] = a1.z; v[7] = a1.w;
+      cb[0] = chunk_bit(b0.x); cb[1] = chunk_bit(b0.y); cb[2] = chunk_bit(b0.z);
+      cb[3] = chunk_bit(b0.w); cb[4] = chunk_bit(b1.x); cb[5] = chunk_bit(b1.y);
+      cb[6] = chunk_bit(b1.z); cb[7] = chunk_bit(b1.w);
+    }
+    const bool full = valid == kBuildTile;
+    // rows that exist from the tile start: rows past the range end but before
+    // n still belong to segments that started in the range
+    const uint32_t exist = left < (uint64_t)kBuildTile ? (uint32_t)left : (uint32_t)kBuildTile;
+    // the row before the thread's first row (row 0 of the column heads a key)
+    uint32_t pv, pc;
+    if (base + first > 0) {
+      pv = wv[kWinBehind + first - 1];
+      pc = wr[kWinBehind + first - 1] / 31;
+    } else {
+      pv = ~v[0];
+      pc = 0;
+    }
+
+    uint32_t headm = 0, vheadm = 0, fills[kBuildItems];
+    uint32_t nw = 0;
+#pragma unroll
+    for (int j = 0; j < kBuildItems; ++j) {
+      const uint32_t c = cb[j] >> 5;
+      const bool ok = full || first + j < valid;
+      const bool vh = v[j] != pv;
+      const bool h = ok && (vh || c != pc);
+      fills[j] = vh ? c : c - pc - 1;
+      if (h) {
+        headm |= 1u << j;
+        if (vh) vheadm |= 1u << j;
+        nw += 1 + (fills[j] != 0);
+      }
+      pv = v[j];
+      pc = c;
+    }
+    const uint32_t nk = __popc(vheadm);
+
+    // Literals: the rows after this thread's last row that continue its last
+    // segment (from the window), then a reverse segmented OR over its rows.
+    uint32_t acc = 0;
+    {
+      const uint32_t v7 = v[kBuildItems - 1], c7 = cb[kBuildItems - 1] >> 5;
+      for (uint32_t m = first + kBuildItems; m < wend; ++m) {
+        const uint32_t rm = wr[kWinBehind + m];
+        if (wv[kWinBehind + m] != v7 || rm / 31 != c7) break;
+        acc |= 1u << (rm % 31);
+      }
+    }
+    uint32_t lits[kBuildItems];
+#pragma unroll
+    for (int j = kBuildItems - 1; j >= 0; --j) {
+      if (first + j < exist) acc |= 1u << (cb[j] & 31);  // rows past n add nothing
+      lits[j] = acc | 0x80000000u;
+      if (headm & (1u << j)) acc = 0;
+    }
+
+    uint64_t tile_agg;
+    const uint64_t my_prefix = block_exclusive_scan64<kBuildThreads>(
+        (uint64_t)nw | ((uint64_t)nk << kPackShift), &tile_agg, sm.warp_tmp);
+    const uint32_t tw = (uint32_t)(tile_agg & kPackMask);
+    const uint32_t tk = (uint32_t)((tile_agg >> kPackShift) & kPackMask);
+
+    uint32_t pw = (uint32_t)(my_prefix & kPackMask);
+    uint32_t pk = (uint32_t)((my_prefix >> kPackShift) & kPackMask);
+#pragma unroll
+    for (int j = 0; j < kBuildItems; ++j) {
+      if (headm & (1u << j)) {
+        if (vheadm & (1u << j)) {
+          sm.keys[skew(pk)] = v[j];
+          sm.offs[skew(pk)] = run_w + pw;
+          ++pk;
+        }
+        if (fills[j]) sm.words[skew(pw++)] = fills[j];
+        sm.words[skew(pw++)] = lits[j];
+      }
+    }
+    __syncthreads();
+
+    if (!sm.abort) {
+      bool overflow = false;
+      for (uint32_t k = tid; k < tw; k += kBuildThreads) {
+        const uint64_t pos = (uint64_t)run_w + k;
+        if (pos < a.index_cap)
+          a.index[pos] = sm.words[skew(k)];
+        else
+          overflow = true;
+      }
+      for (uint32_t k = tid; k < tk; k += kBuildThreads) {
+        const uint64_t pos = (uint64_t)run_k + k;
+        if (pos < a.keys_cap) {
+          a.keys[pos] = sm.keys[skew(k)];
+          a.offsets[pos] = sm.offs[skew(k)];
+        } else {
+          overflow = true;
+        }
+      }
+      if (overflow) set_status(a.status, WAH_EOVERFLOW);
+    }
+    run_w += tw;
+    run_k += tk;
+    __syncthreads();  // staging and window buffer reusable
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Host side.
+// ---------------------------------------------------------------------------
 cudaError_t launch_build(const BuildLaunch& a, cudaStream_t s, uint32_t* launches) {
-  const uint64_t tiles = ceil_div(a.n, kBuildTile);
-  const size_t smem = sizeof(BuildSmem);
+  const size_t smem = sizeof(EmitSmem);
   cudaError_t err =
-      cudaFuncSetAttribute(k_wah_build, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      cudaFuncSetAttribute(k_build_emit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (err != cudaSuccess) return err;
-  err = cudaMemsetAsync(a.lb_build, 0, tiles * sizeof(uint64_t), s);
+  int per_sm = 0;
+  err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_build_emit, kBuildThreads, smem);
+  if (err != cudaSuccess) return err;
+  uint64_t want = (uint64_t)std::max(a.sm_count, 1) * std::max(per_sm, 1);
+  if (want > kMaxRanges) want = kMaxRanges;
+  RangeGeom g;
+  g.range_rows =
+      std::max<uint64_t>(ceil_div(ceil_div(a.n, want), kBuildTile) * kBuildTile, kBuildTile);
+  g.ranges = (uint32_t)std::max<uint64_t>(ceil_div(a.n, g.range_rows), 1);
+
+  err = cudaMemsetAsync(a.range_counts, 0, (size_t)kMaxRanges * 4 * sizeof(uint32_t), s);
   if (err != cudaSuccess) return err;
   record_phase(a.events, kPhaseBuild, false, s);
-  k_wah_build<<<(unsigned)tiles, kBuildThreads, smem, s>>>(
-      a.src, a.sel, a.n, a.ctrl, a.lb_build, a.keys, a.offsets, a.index, a.keys_cap,
-      a.index_cap, a.counts);
+  k_build_count<<<g.ranges * kCountCtasPerRange, kHistThreads, 0, s>>>(a.src, a.sel, a.n, g,
+                                                                       a.ctrl, a.range_counts);
+  k_build_scan<<<1, kBuildScanThreads, 0, s>>>(g.ranges, a.range_counts, a.range_first,
+                                               a.counts);
+  EmitArgs e;
+  e.bufs = a.src;
+  e.sel = a.sel;
+  e.n = a.n;
+  e.g = g;
+  e.ctrl = a.ctrl;
+  e.range_first = a.range_first;
+  e.keys = a.keys;
+  e.offsets = a.offsets;
+  e.index = a.index;
+  e.keys_cap = a.keys_cap;
+  e.index_cap = a.index_cap;
+  e.status = &a.counts->status;
+  k_build_emit<<<g.ranges, kBuildThreads, smem, s>>>(e);
   record_phase(a.events, kPhaseBuild, true, s);
-  ++*launches;
+  *launches += 3;
   return cudaGetLastError();
 }
 

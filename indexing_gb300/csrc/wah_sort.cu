@@ -338,6 +338,7 @@ __global__ void __launch_bounds__(kSortThreads, 2) k_radix_scatter(ScatterArgs a
   const uint32_t lt = lanemask_lt(), gt = lanemask_gt();
   uint32_t* whA = sm.whist[warp][0];
   uint32_t* whB = sm.whist[warp][1];
+  uint32_t phase_bits = 0;  // parity of the next phase of bar[0], bar[1]
 
   for (uint32_t i = 0; i < ntiles; ++i) {
     const uint32_t cur = i & 1;
@@ -357,8 +358,11 @@ __global__ void __launch_bounds__(kSortThreads, 2) k_radix_scatter(ScatterArgs a
     }
     uint32_t key[ITEMS];
     if (valid == TILE) {
-      // i-th use of this buffer's barrier completes phase (i / 2) & 1
-      if (!mbar_wait_bounded(&sm.bar[cur], (i >> 1) & 1)) {
+      // phases of each buffer's barrier complete in turn; the parity of the
+      // next one is tracked per buffer (a tile read with plain loads uses none)
+      const bool ok = mbar_wait_bounded(&sm.bar[cur], (phase_bits >> cur) & 1u);
+      phase_bits ^= 1u << cur;
+      if (!ok) {
         set_status(a.status, WAH_ETIMEOUT);
         sm.abort = 1;
       }

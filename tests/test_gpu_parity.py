@@ -76,6 +76,16 @@ def test_config1_uniform_1m_with_bound(wah):
     assert_same(wah.build_index(v, bound=0), ref, "c1/scan")
 
 
+@pytest.mark.parametrize("kind", ["uniform16", "runs", "two"])
+def test_many_tiles_per_range(wah, kind):
+    # 16M rows: every range owns many tiles, so both halves of each double
+    # buffer are reused many times; the first range's first window is read
+    # without a bulk copy
+    rng = np.random.default_rng(16)
+    v = gen(kind, 1 << 24, rng)
+    assert_same(wah.build_index(v, bound=65535), O.build(v), f"16M/{kind}")
+
+
 def test_sort_phase_matches_stable_sort(wah):
     rng = np.random.default_rng(3)
     for n, m in ((1, 5), (5000, 7), (300_000, 65536), (70_001, 2 ** 32)):
