@@ -15,7 +15,7 @@ namespace {
 
 thread_local uint32_t g_last_launches = 0;
 int g_sort_items = 16;      // onesweep rows per thread (wah_set_tuning)
-bool g_sort_ballot = true;  // peer masks from ballots (wah_set_tuning)
+int g_sort_peers = 0;       // peer-mask mode (wah_set_tuning)
 
 constexpr size_t kAlign = 256;
 inline size_t align_up(size_t x) { return (x + kAlign - 1) / kAlign * kAlign; }
@@ -98,7 +98,7 @@ int enqueue_sort(const uint32_t* d_values, uint64_t n, uint32_t bound, const WsL
   a.status = status;
   a.events = events;
   a.sort_items = g_sort_items;
-  a.sort_ballot = g_sort_ballot;
+  a.sort_peers = g_sort_peers;
   a.sm_count = sm_count_current();
   if (a.sm_count <= 0) return WAH_ENODEV;
   e = launch_sort(a, s, launches);
@@ -147,12 +147,16 @@ uint32_t wah_last_launch_count(void) { return g_last_launches; }
 int wah_set_tuning(int sort_items) {
   const int items = sort_items & 0xff;
   if (items != 8 && items != 12 && items != 16) return WAH_EINVAL;
+  if ((sort_items & WAH_TUNE_MATCH) && (sort_items & WAH_TUNE_HYBRID)) return WAH_EINVAL;
   g_sort_items = items;
-  g_sort_ballot = !(sort_items & WAH_TUNE_MATCH);
+  g_sort_peers = (sort_items & WAH_TUNE_MATCH) ? 1 : (sort_items & WAH_TUNE_HYBRID) ? 2 : 0;
   return WAH_OK;
 }
 
-int wah_get_tuning(void) { return g_sort_items | (g_sort_ballot ? 0 : WAH_TUNE_MATCH); }
+int wah_get_tuning(void) {
+  return g_sort_items | (g_sort_peers == 1 ? WAH_TUNE_MATCH : 0) |
+         (g_sort_peers == 2 ? WAH_TUNE_HYBRID : 0);
+}
 
 static int build_impl(const uint32_t* d_values, uint64_t n, uint32_t bound, uint32_t* d_keys,
                       uint32_t* d_offsets, uint32_t* d_index, wah_counts* d_counts,

@@ -274,7 +274,7 @@ struct SortLaunch {
   uint32_t* status;
   int sm_count;
   int sort_items;       // onesweep rows per thread (8, 12, 16, 20)
-  bool sort_ballot;     // peer masks from ballots instead of match.any
+  int sort_peers;       // peer masks: 0 ballots, 1 match.any, 2 half and half
   cudaEvent_t* events;  // optional: [2*phase] before, [2*phase+1] after
 };
 

@@ -274,7 +274,8 @@ struct ScatterArgs {
   uint32_t* status;
 };
 
-// Lanes of the warp holding the same 8-bit digit as this lane.
+// Lanes of the warp holding the same 8-bit digit as this lane: eight ballots
+// (ALU pipe) or __match_any_sync (MIO pipe).
 template <bool BALLOT>
 __device__ __forceinline__ uint32_t digit_peers(uint32_t d) {
   if (BALLOT) {
@@ -302,7 +303,9 @@ __device__ __forceinline__ void fetch_tile(uint32_t* dst_k, uint32_t* dst_r, uin
   if (rin) bulk_copy_g2s(dst_r, rin + base, bytes, bar);
 }
 
-template <int ITEMS, bool BALLOT>
+// PEERS: 0 all items by ballots, 1 all by match.any, 2 the first half by
+// match.any and the second by ballots (the two pipes work in parallel).
+template <int ITEMS, int PEERS>
 __global__ void __launch_bounds__(kSortThreads, 2) k_radix_scatter(ScatterArgs a) {
   constexpr uint32_t TILE = kSortThreads * ITEMS;
   constexpr int HALF = ITEMS / 2;
@@ -386,7 +389,11 @@ __global__ void __launch_bounds__(kSortThreads, 2) k_radix_scatter(ScatterArgs a
     // Peer masks (independent), then two interleaved counter chains.
     uint32_t rank[ITEMS];
 #pragma unroll
-    for (int j = 0; j < ITEMS; ++j) rank[j] = digit_peers<BALLOT>(bfe(key[j], shift, kRadixBits));
+    for (int j = 0; j < ITEMS; ++j) {
+      const bool ballot = PEERS == 0 || (PEERS == 2 && j >= HALF);
+      rank[j] = ballot ? digit_peers<true>(bfe(key[j], shift, kRadixBits))
+                       : digit_peers<false>(bfe(key[j], shift, kRadixBits));
+    }
 #pragma unroll
     for (int j = 0; j < HALF; ++j) {
       const uint32_t pa = rank[j], pb = rank[j + HALF];
@@ -472,19 +479,19 @@ struct SortVariant {
   size_t smem;
 };
 
-SortVariant sort_variant(int items, bool ballot) {
-  if (ballot) {
-    switch (items) {
-      case 8: return {8, k_radix_scatter<8, true>, sizeof(ScatterSmem<8>)};
-      case 12: return {12, k_radix_scatter<12, true>, sizeof(ScatterSmem<12>)};
-      default: return {16, k_radix_scatter<16, true>, sizeof(ScatterSmem<16>)};
-    }
-  }
+template <int PEERS>
+SortVariant sort_variant_peers(int items) {
   switch (items) {
-    case 8: return {8, k_radix_scatter<8, false>, sizeof(ScatterSmem<8>)};
-    case 12: return {12, k_radix_scatter<12, false>, sizeof(ScatterSmem<12>)};
-    default: return {16, k_radix_scatter<16, false>, sizeof(ScatterSmem<16>)};
+    case 8: return {8, k_radix_scatter<8, PEERS>, sizeof(ScatterSmem<8>)};
+    case 12: return {12, k_radix_scatter<12, PEERS>, sizeof(ScatterSmem<12>)};
+    default: return {16, k_radix_scatter<16, PEERS>, sizeof(ScatterSmem<16>)};
   }
+}
+
+SortVariant sort_variant(int items, int peers) {
+  if (peers == 1) return sort_variant_peers<1>(items);
+  if (peers == 2) return sort_variant_peers<2>(items);
+  return sort_variant_peers<0>(items);
 }
 
 // Equal ranges of whole tiles, one per resident scatter CTA.
@@ -500,7 +507,7 @@ RangeGeom range_geometry(uint64_t n, int resident_ctas, int items) {
 
 cudaError_t launch_sort(const SortLaunch& a, cudaStream_t s, uint32_t* launches) {
   const uint64_t n = a.n;
-  const SortVariant v = sort_variant(a.sort_items, a.sort_ballot);
+  const SortVariant v = sort_variant(a.sort_items, a.sort_peers);
   cudaError_t err =
       cudaFuncSetAttribute(v.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)v.smem);
   if (err != cudaSuccess) return err;

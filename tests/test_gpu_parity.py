@@ -137,7 +137,8 @@ def test_decoded_bitmaps_match_rows(wah):
         assert [j for j, ch in enumerate(s) if ch == "1"] == rows.tolist()
 
 
-@pytest.mark.parametrize("items", [8, 12, 16, 8 | 0x100, 12 | 0x100, 16 | 0x100])
+@pytest.mark.parametrize("items", [8, 12, 16, 8 | 0x100, 12 | 0x100, 16 | 0x100,
+                                   8 | 0x200, 16 | 0x200])
 def test_every_sort_tile_shape(wah, items):
     lib = wah._lib.load()
     old = lib.wah_get_tuning()
@@ -155,3 +156,4 @@ def test_every_sort_tile_shape(wah, items):
 def test_rejects_unknown_tuning(wah):
     assert wah._lib.load().wah_set_tuning(7) == wah.WAH_EINVAL
     assert wah._lib.load().wah_set_tuning(20) == wah.WAH_EINVAL
+    assert wah._lib.load().wah_set_tuning(16 | 0x300) == wah.WAH_EINVAL
