@@ -12,8 +12,9 @@ SHOW_TIME_CONSUMPTION output, src/phases.cpp:714-1127) go to stderr.
   value       rows/s with the column resident in HBM (CUDA events around K
               builds on the launching stream; the 1 GiB input and 6+ GiB of
               traffic per build exceed the 129 MB L2, so no flush is needed)
-  e2e         rows/s through wah_ctx_build_host with pinned host buffers:
-              H2D of the values, build, D2H of keys/offsets/index, per step
+  e2e         rows/s through the pipelined host-buffer API (wah_pipe_*) with
+              pinned host buffers: H2D of the values, build, D2H of
+              keys/offsets/index, every step; consecutive steps overlap
   roofline    the dominant kernel's algorithmic bytes / its mean event-timed
               duration, against the measured HBM copy bandwidth
   cpu_baseline  the oracle (plain-C restatement of the reference `cpu`
@@ -55,6 +56,8 @@ def parse():
     ap.add_argument("--card", type=int, default=65536, help="values uniform in [0, card)")
     ap.add_argument("--seed", type=int, default=20170101)
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--pipe-depth", type=int, default=3,
+                    help="builds in flight in the end-to-end leg")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--sort-items", type=int, default=0,
                     help="onesweep rows per thread (0: library default)")
@@ -299,45 +302,39 @@ def main():
             gbs = alg[p] / (phase_ms[p] / 1e3) / 1e9 if phase_ms[p] > 0 and alg[p] else 0
             print(f"{p}:\t{phase_ms[p] * 1e3:.0f} us\t{gbs:.0f} GB/s", file=sys.stderr)
 
-    # End to end: host values in, host index out, through the C ABI context.
+    # End to end: host values in, host index out, through the public
+    # pipelined host-buffer API (wah_pipe_*): every step copies its column in
+    # from pinned host memory and its keys/offsets/index out to pinned host
+    # memory; consecutive steps overlap (depth builds in flight).
     e2e = None
     if not args.no_e2e:
         pin_v = torch.empty(n, dtype=torch.int32, pin_memory=True)
         pin_v.numpy()[:] = values_np.view(np.int32)
-        kc, ic = wah.output_caps(n, bound)
-        pin_k = torch.empty(kc, dtype=torch.int32, pin_memory=True)
-        pin_o = torch.empty(kc, dtype=torch.int32, pin_memory=True)
-        pin_i = torch.empty(ic, dtype=torch.int32, pin_memory=True)
         del bufs  # free the device-resident run's buffers
         torch.cuda.empty_cache()
-        ctx = wah.HostContext(n, bound)
-        cnt = wah.wah_counts()
+        pipe = wah.Pipeline(n, bound, depth=args.pipe_depth)
         e2e_steps = max(3, min(args.steps, 20))
-
-        def e2e_step():
-            rc = lib.wah_ctx_build_host(ctx._h, pin_v.data_ptr(), n, pin_k.data_ptr(),
-                                        pin_o.data_ptr(), pin_i.data_ptr(), ctypes.byref(cnt))
-            if rc != 0:
-                raise wah.WahError(rc, "wah_ctx_build_host")
-
         for _ in range(max(1, args.warmup)):
-            e2e_step()
+            pipe.result(pipe.submit(pin_v))
         if dist:
             dist.barrier()
         t0 = time.perf_counter()
-        for _ in range(e2e_steps):
-            e2e_step()
+        tickets = [pipe.submit(pin_v) for _ in range(e2e_steps)]
+        for t in tickets[:-1]:
+            pipe.wait(t)
+        last = pipe.result(tickets[-1])
         dt = time.perf_counter() - t0
         if dist:
             t = torch.tensor([dt], device=dev, dtype=torch.float64)
             dist.all_reduce(t, op=dist.ReduceOp.MAX)
             dt = float(t.item())
-        assert cnt.keycnt == K and cnt.index_len == L
+        assert last.keycnt == K and last.index_len == L and last.merged == k
         e2e = {"value": world * n * e2e_steps / dt, "unit": "rows/s",
                "h2d_bytes_per_step": 4 * n,
-               "d2h_bytes_per_step": 16 + 8 * cnt.keycnt + 4 * cnt.index_len,
-               "ms_per_step": 1e3 * dt / e2e_steps, "steps": e2e_steps}
-        ctx.close()
+               "d2h_bytes_per_step": 16 + 8 * K + 4 * L,
+               "ms_per_step": 1e3 * dt / e2e_steps, "steps": e2e_steps,
+               "pipeline_depth": args.pipe_depth}
+        pipe.close()
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

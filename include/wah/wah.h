@@ -149,6 +149,32 @@ int wah_ctx_build_host(wah_ctx* ctx, const uint32_t* h_values, uint64_t n,
                        wah_counts* h_counts);
 void wah_ctx_destroy(wah_ctx* ctx);
 
+/*
+ * Pipelined host-buffer builds: the reference's per-column flow
+ * (global_argument -> phases -> mem_ref::data, src/phases.cpp:720-1088) with
+ * several columns in flight, like `gpu --jobs` (src/gpu.cpp:194-259).  A pipe
+ * owns `depth` (1..8) slots of device buffers for columns of up to max_n
+ * rows, each with its own stream, and a completion thread.  wah_pipe_submit
+ * enqueues the copy of h_values in and the build, and returns a ticket
+ * without waiting (unless every slot is busy: then it first waits for the
+ * oldest build); the completion thread copies exactly keys[K], offsets[K],
+ * index[L] and the counters out once the build's sizes are known.
+ * Consecutive submits overlap on the GPU and on the host link.  h_values
+ * must stay unchanged, and the output buffers (capacities as
+ * wah_output_caps) untouched, until wah_pipe_wait(ticket) returns; the
+ * outputs are valid when it returns WAH_OK and h_counts->status == WAH_OK.
+ * Pinned host buffers (cudaHostAlloc / cudaMallocHost / cudaHostRegister)
+ * copy fastest; pageable ones work.  A pipe is driven by one host thread.
+ */
+typedef struct wah_pipe wah_pipe;
+int wah_pipe_create(uint64_t max_n, uint32_t bound, uint32_t depth,
+                    wah_pipe** out);
+int wah_pipe_submit(wah_pipe* pipe, const uint32_t* h_values, uint64_t n,
+                    uint32_t* h_keys, uint32_t* h_offsets, uint32_t* h_index,
+                    wah_counts* h_counts, uint64_t* ticket);
+int wah_pipe_wait(wah_pipe* pipe, uint64_t ticket);
+void wah_pipe_destroy(wah_pipe* pipe);
+
 /* Number of kernels the last wah_build/wah_ctx_build_host on this thread
  * enqueued (launch accounting for benchmarks). */
 uint32_t wah_last_launch_count(void);

@@ -29,7 +29,7 @@ from . import _lib
 from ._lib import wah_counts
 
 __all__ = ["WahError", "WahIndex", "build_index", "sort_rids_by_value", "build_sorted",
-           "HostContext", "decoded_bitmap", "workspace_bytes", "output_caps",
+           "HostContext", "Pipeline", "decoded_bitmap", "workspace_bytes", "output_caps",
            "MAX_ROWS", "last_launch_count"]
 
 MAX_ROWS = 1 << 30
@@ -255,6 +255,84 @@ class HostContext:
         index = np.empty(self.index_cap, np.uint32)
         c = self.build_into(values, keys, offs, index)
         return WahIndex(keys[:c.keycnt], offs[:c.keycnt], index[:c.index_len], c.merged)
+
+
+class Pipeline:
+    """Several host-buffer builds in flight (``wah_pipe_*``).
+
+    ``submit`` copies a column in, builds it and copies its index out into
+    pinned host buffers owned by this object (one set per slot), without
+    waiting; ``result(ticket)`` waits for one build and returns numpy views of
+    its outputs (valid until the slot is reused ``depth`` submits later).
+    """
+
+    def __init__(self, max_n: int, bound: int = 0, depth: int = 3):
+        torch = _torch()
+        self._lib = _lib.load()
+        h = ctypes.c_void_p()
+        _check(self._lib.wah_pipe_create(max_n, bound, depth, ctypes.byref(h)),
+               "wah_pipe_create")
+        self._h = h
+        self.depth = depth
+        kc, ic = output_caps(max(max_n, 1), bound)
+        self._out = []
+        for _ in range(depth):
+            self._out.append(dict(
+                keys=torch.empty(kc, dtype=torch.int32, pin_memory=True),
+                offsets=torch.empty(kc, dtype=torch.int32, pin_memory=True),
+                index=torch.empty(ic, dtype=torch.int32, pin_memory=True),
+                counts=torch.zeros(4, dtype=torch.int32, pin_memory=True)))
+        self._slot_of = {}
+        self._next = 0
+
+    def submit(self, values) -> int:
+        """values: pinned uint32/int32 host tensor or numpy array (kept alive
+        by the caller until the result is taken)."""
+        if hasattr(values, "data_ptr"):
+            ptr, n = values.data_ptr(), values.numel()
+        else:
+            ptr, n = values.ctypes.data, values.size
+        slot = self._next % self.depth  # the pipe fills its slots round robin
+        o = self._out[slot]
+        t = ctypes.c_uint64()
+        _check(self._lib.wah_pipe_submit(self._h, ptr, n, o["keys"].data_ptr(),
+                                         o["offsets"].data_ptr(), o["index"].data_ptr(),
+                                         o["counts"].data_ptr(), ctypes.byref(t)),
+               "wah_pipe_submit")
+        self._next += 1
+        self._slot_of[t.value] = slot
+        return t.value
+
+    def wait(self, ticket: int) -> None:
+        _check(self._lib.wah_pipe_wait(self._h, ticket), "wah_pipe_wait")
+
+    def result(self, ticket: int) -> WahIndex:
+        self.wait(ticket)
+        o = self._out[self._slot_of.pop(ticket)]
+        c = o["counts"].numpy().view(np.uint32)
+        if c[3] != WAH_OK:
+            raise WahError(int(c[3]), "pipeline build (device)")
+        K, L = int(c[0]), int(c[1])
+        return WahIndex(o["keys"].numpy().view(np.uint32)[:K],
+                        o["offsets"].numpy().view(np.uint32)[:K],
+                        o["index"].numpy().view(np.uint32)[:L], int(c[2]))
+
+    def close(self):
+        if self._h:
+            self._lib.wah_pipe_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
 
 
 def decoded_bitmap(words) -> str:

@@ -19,7 +19,7 @@ INCLUDE = os.path.join(REPO_DIR, "include")
 OBJ_DIR = os.path.join(PKG_DIR, "_build")
 LIB_PATH = os.path.join(PKG_DIR, "libwah_gb300.so")
 
-CUDA_SOURCES = ["wah_sort.cu", "wah_index.cu", "wah_api.cu", "wah_noalloc.cu"]
+CUDA_SOURCES = ["wah_sort.cu", "wah_index.cu", "wah_api.cu", "wah_pipe.cu", "wah_noalloc.cu"]
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo",
               "-std=c++17", "-Xcompiler", "-fPIC", "-I" + INCLUDE, "-I" + CSRC]
 
@@ -83,6 +83,11 @@ SIGNATURES = {
     "wah_ctx_build_host": ([_vp, _vp, _u64, _vp, _vp, _vp, ctypes.POINTER(wah_counts)],
                            ctypes.c_int),
     "wah_ctx_destroy": ([_vp], None),
+    "wah_pipe_create": ([_u64, _u32, _u32, ctypes.POINTER(_vp)], ctypes.c_int),
+    "wah_pipe_submit": ([_vp, _vp, _u64, _vp, _vp, _vp, _vp, ctypes.POINTER(_u64)],
+                        ctypes.c_int),
+    "wah_pipe_wait": ([_vp, _u64], ctypes.c_int),
+    "wah_pipe_destroy": ([_vp], None),
     "wah_last_launch_count": ([], _u32),
     "wah_set_tuning": ([ctypes.c_int], ctypes.c_int),
     "wah_get_tuning": ([], ctypes.c_int),

@@ -1,5 +1,7 @@
 """Parity of the CUDA path (through the C ABI) with the oracle and with the
 golden vectors made by the reference's own code.  Integer work: bit-exact."""
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -157,3 +159,55 @@ def test_rejects_unknown_tuning(wah):
     assert wah._lib.load().wah_set_tuning(7) == wah.WAH_EINVAL
     assert wah._lib.load().wah_set_tuning(20) == wah.WAH_EINVAL
     assert wah._lib.load().wah_set_tuning(16 | 0x300) == wah.WAH_EINVAL
+
+
+def test_pipeline_matches_oracle(wah):
+    # several columns in flight; every result equals the oracle's
+    rng = np.random.default_rng(21)
+    cols = [gen(k, n, rng) for k, n in (("uniform16", 300_000), ("runs", 1 << 20),
+                                        ("few16", 77_777), ("zipf", 500_000),
+                                        ("two", 4097), ("const", 1))]
+    pinned = []
+    for v in cols:
+        t = torch.empty(v.size, dtype=torch.int32, pin_memory=True)
+        t.numpy()[:] = v.view(np.int32)
+        pinned.append(t)
+    with wah.Pipeline(1 << 20, bound=65535, depth=3) as pipe:
+        tickets = []
+        for i, t in enumerate(pinned):
+            tickets.append(pipe.submit(t))
+            if i >= 2:  # take results while later columns are in flight
+                j = i - 2
+                r = pipe.result(tickets[j])
+                ref = O.build(cols[j])
+                assert np.array_equal(r.keys, ref.keys) and np.array_equal(r.index, ref.index)
+                assert np.array_equal(r.offsets, ref.offsets)
+        for j in range(len(pinned) - 2, len(pinned)):
+            r = pipe.result(tickets[j])
+            ref = O.build(cols[j])
+            assert np.array_equal(r.keys, ref.keys) and np.array_equal(r.index, ref.index)
+
+
+def test_pipeline_pageable_buffers_and_errors(wah):
+    lib = wah._lib.load()
+    h = ctypes.c_void_p()
+    assert lib.wah_pipe_create(1024, 0, 2, ctypes.byref(h)) == 0
+    try:
+        v = np.arange(100, 0, -1, dtype=np.uint32)
+        keys = np.empty(1024, np.uint32)
+        offs = np.empty(1024, np.uint32)
+        index = np.empty(2048, np.uint32)
+        cnt = np.zeros(4, dtype=np.uint32)
+        t = ctypes.c_uint64()
+        assert lib.wah_pipe_submit(h, v.ctypes.data, 100, keys.ctypes.data, offs.ctypes.data,
+                                   index.ctypes.data, cnt.ctypes.data, ctypes.byref(t)) == 0
+        assert lib.wah_pipe_wait(h, t.value) == 0
+        ref = O.build(v)
+        assert cnt[3] == 0 and cnt[0] == len(ref.keys) and cnt[1] == len(ref.index)
+        assert np.array_equal(index[:cnt[1]], ref.index)
+        # too long for the pipe
+        assert lib.wah_pipe_submit(h, v.ctypes.data, 2000, keys.ctypes.data, offs.ctypes.data,
+                                   index.ctypes.data, cnt.ctypes.data,
+                                   ctypes.byref(t)) == wah.WAH_ERANGE
+    finally:
+        lib.wah_pipe_destroy(h)
