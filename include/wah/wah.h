@@ -150,6 +150,43 @@ int wah_ctx_build_host(wah_ctx* ctx, const uint32_t* h_values, uint64_t n,
 void wah_ctx_destroy(wah_ctx* ctx);
 
 /*
+ * Batched builds: many columns, each indexed exactly as wah_build would index
+ * it alone, with every kernel of the pipeline launched once for the whole
+ * batch (the reference's single-kernel batch path, kernel_wah_index in
+ * include/kernel_wah_bitindex.cl:43-91 driven by src/gpu.cpp:194-259,
+ * indexes each <=1,023-row batch separately).  wah_batch_create plans a batch
+ * for given row counts and bounds (host arrays) and allocates its device
+ * memory; wah_batch_set_columns sets the columns' device buffers (their n and
+ * bound must match the plan; values 16-byte aligned; outputs with
+ * wah_output_caps capacities; counts 16-byte aligned) by an upload enqueued
+ * on `stream`; wah_batch_build enqueues the build (no allocation, no host
+ * synchronisation); wah_batch_launch_graph captures that build into a CUDA
+ * graph on its first call and replays it, so new columns of the same sizes
+ * need only wah_batch_set_columns + a replay.  Results and errors are in each
+ * column's counts.
+ */
+typedef struct wah_column {
+  const uint32_t* values; /* device, n values                         */
+  uint64_t n;
+  uint32_t bound;         /* largest value, 0 = unknown               */
+  uint32_t reserved;
+  uint32_t* keys;         /* device outputs                           */
+  uint32_t* offsets;
+  uint32_t* index;
+  wah_counts* counts;     /* device                                   */
+} wah_column;
+
+typedef struct wah_batch wah_batch;
+int wah_batch_create(const uint64_t* ns, const uint32_t* bounds, uint32_t ncols,
+                     wah_batch** out);
+int wah_batch_set_columns(wah_batch* batch, const wah_column* cols, void* stream);
+int wah_batch_build(wah_batch* batch, void* stream);
+int wah_batch_launch_graph(wah_batch* batch, void* stream);
+size_t wah_batch_device_bytes(const wah_batch* batch);
+uint32_t wah_batch_ranges(const wah_batch* batch);
+void wah_batch_destroy(wah_batch* batch);
+
+/*
  * Pipelined host-buffer builds: the reference's per-column flow
  * (global_argument -> phases -> mem_ref::data, src/phases.cpp:720-1088) with
  * several columns in flight, like `gpu --jobs` (src/gpu.cpp:194-259).  A pipe

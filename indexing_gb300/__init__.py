@@ -29,7 +29,7 @@ from . import _lib
 from ._lib import wah_counts
 
 __all__ = ["WahError", "WahIndex", "build_index", "sort_rids_by_value", "build_sorted",
-           "HostContext", "Pipeline", "decoded_bitmap", "workspace_bytes", "output_caps",
+           "HostContext", "Pipeline", "Batch", "decoded_bitmap", "workspace_bytes", "output_caps",
            "MAX_ROWS", "last_launch_count"]
 
 MAX_ROWS = 1 << 30
@@ -255,6 +255,101 @@ class HostContext:
         index = np.empty(self.index_cap, np.uint32)
         c = self.build_into(values, keys, offs, index)
         return WahIndex(keys[:c.keycnt], offs[:c.keycnt], index[:c.index_len], c.merged)
+
+
+class Batch:
+    """Many device columns built by one launch sequence (``wah_batch_*``).
+
+    ``Batch(sizes, bounds)`` plans the batch; ``set_columns(values)`` takes a
+    list of CUDA int32 tensors with those sizes and allocates their outputs;
+    ``build()`` (or ``launch_graph()``, a replayed CUDA graph) enqueues the
+    build; ``results()`` returns one :class:`WahIndex` per column.
+    """
+
+    def __init__(self, sizes, bounds=None):
+        self._lib = _lib.load()
+        self.sizes = [int(x) for x in sizes]
+        self.bounds = [int(x) for x in (bounds if bounds is not None else [0] * len(self.sizes))]
+        nc = len(self.sizes)
+        ns = (ctypes.c_uint64 * nc)(*self.sizes)
+        bs = (ctypes.c_uint32 * nc)(*self.bounds)
+        h = ctypes.c_void_p()
+        _check(self._lib.wah_batch_create(ns, bs, nc, ctypes.byref(h)), "wah_batch_create")
+        self._h = h
+        self._cols = None
+        self._keep = None
+
+    @property
+    def device_bytes(self) -> int:
+        return int(self._lib.wah_batch_device_bytes(self._h))
+
+    @property
+    def ranges(self) -> int:
+        return int(self._lib.wah_batch_ranges(self._h))
+
+    def set_columns(self, values, stream=None, outputs=None):
+        """values: list of CUDA int32 tensors; outputs: optional list of
+        (keys, offsets, index, counts) CUDA int32 tensors to reuse."""
+        torch = _torch()
+        nc = len(self.sizes)
+        if len(values) != nc:
+            raise ValueError("one tensor per planned column")
+        cols = (_lib.wah_column * nc)()
+        outs = []
+        for c, v in enumerate(values):
+            if v.numel() != self.sizes[c]:
+                raise ValueError(f"column {c}: {v.numel()} rows, planned {self.sizes[c]}")
+            if outputs is not None:
+                keys, offs, index, counts = outputs[c]
+            else:
+                kc, ic = output_caps(max(self.sizes[c], 1), self.bounds[c])
+                keys = torch.empty(kc, dtype=torch.int32, device=v.device)
+                offs = torch.empty(kc, dtype=torch.int32, device=v.device)
+                index = torch.empty(ic, dtype=torch.int32, device=v.device)
+                counts = torch.zeros(4, dtype=torch.int32, device=v.device)
+            outs.append((keys, offs, index, counts))
+            cols[c].values = v.data_ptr()
+            cols[c].n = self.sizes[c]
+            cols[c].bound = self.bounds[c]
+            cols[c].keys = keys.data_ptr()
+            cols[c].offsets = offs.data_ptr()
+            cols[c].index = index.data_ptr()
+            cols[c].counts = counts.data_ptr()
+        _check(self._lib.wah_batch_set_columns(self._h, cols, _stream_handle(stream)),
+               "wah_batch_set_columns")
+        self._cols = outs
+        self._keep = list(values)
+        return outs
+
+    def build(self, stream=None):
+        _check(self._lib.wah_batch_build(self._h, _stream_handle(stream)), "wah_batch_build")
+
+    def launch_graph(self, stream=None):
+        _check(self._lib.wah_batch_launch_graph(self._h, _stream_handle(stream)),
+               "wah_batch_launch_graph")
+
+    def results(self):
+        torch = _torch()
+        torch.cuda.synchronize()
+        out = []
+        counts = torch.stack([o[3] for o in self._cols]).cpu().numpy().view(np.uint32)
+        for c, (keys, offs, index, _) in enumerate(self._cols):
+            K, L, k, st = (int(x) for x in counts[c])
+            if st != WAH_OK:
+                raise WahError(st, f"batched build, column {c}")
+            out.append(WahIndex(keys[:K], offs[:K], index[:L], k))
+        return out
+
+    def close(self):
+        if self._h:
+            self._lib.wah_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class Pipeline:

@@ -19,7 +19,8 @@ INCLUDE = os.path.join(REPO_DIR, "include")
 OBJ_DIR = os.path.join(PKG_DIR, "_build")
 LIB_PATH = os.path.join(PKG_DIR, "libwah_gb300.so")
 
-CUDA_SOURCES = ["wah_sort.cu", "wah_index.cu", "wah_api.cu", "wah_pipe.cu", "wah_noalloc.cu"]
+CUDA_SOURCES = ["wah_sort.cu", "wah_index.cu", "wah_api.cu", "wah_batch.cu", "wah_pipe.cu",
+                "wah_noalloc.cu"]
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo",
               "-std=c++17", "-Xcompiler", "-fPIC", "-I" + INCLUDE, "-I" + CSRC]
 
@@ -64,6 +65,13 @@ class wah_counts(ctypes.Structure):
                 ("merged", ctypes.c_uint32), ("status", ctypes.c_uint32)]
 
 
+class wah_column(ctypes.Structure):
+    _fields_ = [("values", ctypes.c_void_p), ("n", ctypes.c_uint64), ("bound", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32), ("keys", ctypes.c_void_p),
+                ("offsets", ctypes.c_void_p), ("index", ctypes.c_void_p),
+                ("counts", ctypes.c_void_p)]
+
+
 # Exported symbols and their signatures (must match include/wah/wah.h).
 _vp = ctypes.c_void_p
 _u64 = ctypes.c_uint64
@@ -83,6 +91,14 @@ SIGNATURES = {
     "wah_ctx_build_host": ([_vp, _vp, _u64, _vp, _vp, _vp, ctypes.POINTER(wah_counts)],
                            ctypes.c_int),
     "wah_ctx_destroy": ([_vp], None),
+    "wah_batch_create": ([ctypes.POINTER(_u64), ctypes.POINTER(_u32), _u32,
+                          ctypes.POINTER(_vp)], ctypes.c_int),
+    "wah_batch_set_columns": ([_vp, _vp, _vp], ctypes.c_int),
+    "wah_batch_build": ([_vp, _vp], ctypes.c_int),
+    "wah_batch_launch_graph": ([_vp, _vp], ctypes.c_int),
+    "wah_batch_device_bytes": ([_vp], ctypes.c_size_t),
+    "wah_batch_ranges": ([_vp], _u32),
+    "wah_batch_destroy": ([_vp], None),
     "wah_pipe_create": ([_u64, _u32, _u32, ctypes.POINTER(_vp)], ctypes.c_int),
     "wah_pipe_submit": ([_vp, _vp, _u64, _vp, _vp, _vp, _vp, ctypes.POINTER(_u64)],
                         ctypes.c_int),

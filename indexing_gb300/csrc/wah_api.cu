@@ -11,42 +11,12 @@
 #include "wah_common.cuh"
 
 namespace wah {
-namespace {
 
 thread_local uint32_t g_last_launches = 0;
-int g_sort_items = 16;      // onesweep rows per thread (wah_set_tuning)
-int g_sort_peers = 0;       // peer-mask mode (wah_set_tuning)
+int g_sort_items = 16;  // radix tile rows per thread (wah_set_tuning)
+int g_sort_peers = 0;   // peer-mask mode (wah_set_tuning)
 
-constexpr size_t kAlign = 256;
-inline size_t align_up(size_t x) { return (x + kAlign - 1) / kAlign * kAlign; }
-
-struct WsLayout {
-  size_t ctrl, range_hist, range_start, lb_build, keys_a, rids_a, keys_b, rids_b, total;
-};
-
-WsLayout ws_layout(uint64_t n) {
-  WsLayout l;
-  size_t off = 0;
-  l.ctrl = off;
-  off += align_up(sizeof(WahCtrl));
-  l.range_hist = off;
-  off += align_up((size_t)kDigits * kMaxRanges * kRadix * sizeof(uint32_t));
-  l.range_start = off;
-  off += align_up((size_t)kMaxRanges * kRadix * sizeof(uint32_t));
-  l.lb_build = off;
-  off += align_up((size_t)kMaxRanges * 6 * sizeof(uint32_t));
-  const size_t col = align_up(std::max<uint64_t>(n, 1) * sizeof(uint32_t));
-  l.keys_a = off;
-  off += col;
-  l.rids_a = off;
-  off += col;
-  l.keys_b = off;
-  off += col;
-  l.rids_b = off;
-  off += col;
-  l.total = off;
-  return l;
-}
+uint32_t* last_launches_slot() { return &g_last_launches; }
 
 int passes_for_bound(uint32_t bound) {
   if (bound == 0) return kDigits;  // unknown: plan on the device, skip trivial digits
@@ -65,8 +35,6 @@ int sm_count_current() {
   return sms;
 }
 
-inline bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
-
 int cuda_status(cudaError_t e) {
   if (e == cudaSuccess) return WAH_OK;
   if (e == cudaErrorMemoryAllocation) return WAH_ENOMEM;
@@ -76,40 +44,70 @@ int cuda_status(cudaError_t e) {
   return WAH_ECUDA;
 }
 
-// Sort into the workspace ping-pong buffers; the final home is chosen on the
-// device (WahCtrl::final_sel).
-int enqueue_sort(const uint32_t* d_values, uint64_t n, uint32_t bound, const WsLayout& l,
-                 unsigned char* ws, uint32_t* status, cudaStream_t s, uint32_t* launches,
-                 SortBufs* bufs_out, cudaEvent_t* events = nullptr) {
-  WahCtrl* ctrl = reinterpret_cast<WahCtrl*>(ws + l.ctrl);
-  cudaError_t e = cudaMemsetAsync(ctrl, 0, sizeof(WahCtrl), s);
-  if (e != cudaSuccess) return cuda_status(e);
-  SortLaunch a;
-  a.values = d_values;
-  a.n = n;
-  a.passes = passes_for_bound(bound);
-  a.ctrl = ctrl;
-  a.range_hist = reinterpret_cast<uint32_t*>(ws + l.range_hist);
-  a.range_start = reinterpret_cast<uint32_t*>(ws + l.range_start);
-  a.buf_keys[0] = reinterpret_cast<uint32_t*>(ws + l.keys_a);
-  a.buf_rids[0] = reinterpret_cast<uint32_t*>(ws + l.rids_a);
-  a.buf_keys[1] = reinterpret_cast<uint32_t*>(ws + l.keys_b);
-  a.buf_rids[1] = reinterpret_cast<uint32_t*>(ws + l.rids_b);
-  a.status = status;
-  a.events = events;
-  a.sort_items = g_sort_items;
-  a.sort_peers = g_sort_peers;
-  a.sm_count = sm_count_current();
-  if (a.sm_count <= 0) return WAH_ENODEV;
-  e = launch_sort(a, s, launches);
-  if (e != cudaSuccess) return cuda_status(e);
-  bufs_out->keys[kSelInput] = d_values;
-  bufs_out->rids[kSelInput] = nullptr;
-  bufs_out->keys[kSelA] = a.buf_keys[0];
-  bufs_out->rids[kSelA] = a.buf_rids[0];
-  bufs_out->keys[kSelB] = a.buf_keys[1];
-  bufs_out->rids[kSelB] = a.buf_rids[1];
-  return WAH_OK;
+LaunchOpts launch_opts(int max_passes, cudaEvent_t* events) {
+  LaunchOpts o;
+  o.sort_items = g_sort_items;
+  o.sort_peers = g_sort_peers;
+  o.max_passes = max_passes;
+  o.sm_count = sm_count_current();
+  o.events = events;
+  return o;
+}
+
+namespace {
+
+constexpr size_t kAlign = 256;
+inline size_t align_up(size_t x) { return (x + kAlign - 1) / kAlign * kAlign; }
+
+struct WsLayout {
+  size_t ctrl, range_hist, range_start, range_counts, range_first, keys_a, rids_a, keys_b,
+      rids_b, total;
+};
+
+WsLayout ws_layout(uint64_t n) {
+  WsLayout l;
+  size_t off = 0;
+  l.ctrl = off;
+  off += align_up(sizeof(WahCtrl));
+  l.range_hist = off;
+  off += align_up((size_t)kDigits * kMaxRanges * kRadix * sizeof(uint32_t));
+  l.range_start = off;
+  off += align_up((size_t)kMaxRanges * kRadix * sizeof(uint32_t));
+  l.range_counts = off;
+  off += align_up((size_t)kMaxRanges * 4 * sizeof(uint32_t));
+  l.range_first = off;
+  off += align_up((size_t)kMaxRanges * 2 * sizeof(uint32_t));
+  const size_t col = align_up(std::max<uint64_t>(n, 1) * sizeof(uint32_t));
+  l.keys_a = off;
+  off += col;
+  l.rids_a = off;
+  off += col;
+  l.keys_b = off;
+  off += col;
+  l.rids_b = off;
+  off += col;
+  l.total = off;
+  return l;
+}
+
+inline bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
+
+// The column view and range arrays of one build inside a workspace.
+void workspace_views(const WsLayout& l, unsigned char* ws, uint64_t n, ColumnView* c,
+                     RangeArrays* ra) {
+  std::memset(c, 0, sizeof(*c));
+  c->n = n;
+  c->ctrl = reinterpret_cast<WahCtrl*>(ws + l.ctrl);
+  c->keys_a = reinterpret_cast<uint32_t*>(ws + l.keys_a);
+  c->rids_a = reinterpret_cast<uint32_t*>(ws + l.rids_a);
+  c->keys_b = reinterpret_cast<uint32_t*>(ws + l.keys_b);
+  c->rids_b = reinterpret_cast<uint32_t*>(ws + l.rids_b);
+  c->fixed_sel = -1;
+  ra->hist = reinterpret_cast<uint32_t*>(ws + l.range_hist);
+  ra->start = reinterpret_cast<uint32_t*>(ws + l.range_start);
+  ra->counts = reinterpret_cast<uint32_t*>(ws + l.range_counts);
+  ra->first = reinterpret_cast<uint32_t*>(ws + l.range_first);
+  ra->max_ranges = kMaxRanges;
 }
 
 }  // namespace
@@ -173,28 +171,24 @@ static int build_impl(const uint32_t* d_values, uint64_t n, uint32_t bound, uint
   if (!aligned16(d_values) || !aligned16(d_workspace)) return WAH_EINVAL;
   const WsLayout l = ws_layout(n);
   if (workspace_bytes < l.total) return WAH_ENOMEM;
-  unsigned char* ws = static_cast<unsigned char*>(d_workspace);
-
-  SortBufs bufs;
-  int rc = enqueue_sort(d_values, n, bound, l, ws, &d_counts->status, s, &g_last_launches, &bufs,
-                        events);
-  if (rc != WAH_OK) return rc;
-
-  BuildLaunch b;
-  b.events = events;
-  b.src = bufs;
-  b.sel = -1;
-  b.n = n;
-  b.ctrl = reinterpret_cast<WahCtrl*>(ws + l.ctrl);
-  b.range_counts = reinterpret_cast<uint32_t*>(ws + l.lb_build);
-  b.range_first = b.range_counts + kMaxRanges * 4;
-  b.sm_count = sm_count_current();
-  b.keys = d_keys;
-  b.offsets = d_offsets;
-  b.index = d_index;
-  wah_output_caps(n, bound, &b.keys_cap, &b.index_cap);
-  b.counts = d_counts;
-  return cuda_status(launch_build(b, s, &g_last_launches));
+  ColumnView c;
+  RangeArrays ra;
+  workspace_views(l, static_cast<unsigned char*>(d_workspace), n, &c, &ra);
+  c.input = d_values;
+  c.keys = d_keys;
+  c.offsets = d_offsets;
+  c.index = d_index;
+  wah_output_caps(n, bound, &c.keys_cap, &c.index_cap);
+  c.counts = d_counts;
+  c.status = &d_counts->status;
+  c.passes = passes_for_bound(bound);
+  const LaunchOpts o = launch_opts(c.passes, events);
+  if (o.sm_count <= 0) return WAH_ENODEV;
+  e = cudaMemsetAsync(c.ctrl, 0, sizeof(WahCtrl), s);
+  if (e != cudaSuccess) return cuda_status(e);
+  e = launch_sort_one(c, ra, o, s, &g_last_launches);
+  if (e != cudaSuccess) return cuda_status(e);
+  return cuda_status(launch_build_one(c, ra, o, s, &g_last_launches));
 }
 
 int wah_build(const uint32_t* d_values, uint64_t n, uint32_t bound, uint32_t* d_keys,
@@ -250,15 +244,20 @@ int wah_sort_rids_by_value(const uint32_t* d_values, uint64_t n, uint32_t bound,
   if (!aligned16(d_values) || !aligned16(d_workspace)) return WAH_EINVAL;
   const WsLayout l = ws_layout(n);
   if (workspace_bytes < l.total) return WAH_ENOMEM;
-  unsigned char* ws = static_cast<unsigned char*>(d_workspace);
-  SortBufs bufs;
-  int rc = enqueue_sort(d_values, n, bound, l, ws, d_status, s, &g_last_launches, &bufs);
-  if (rc != WAH_OK) return rc;
+  ColumnView c;
+  RangeArrays ra;
+  workspace_views(l, static_cast<unsigned char*>(d_workspace), n, &c, &ra);
+  c.input = d_values;
+  c.status = d_status;
+  c.passes = passes_for_bound(bound);
+  const LaunchOpts o = launch_opts(c.passes, nullptr);
+  if (o.sm_count <= 0) return WAH_ENODEV;
+  cudaError_t e = cudaMemsetAsync(c.ctrl, 0, sizeof(WahCtrl), s);
+  if (e != cudaSuccess) return cuda_status(e);
+  e = launch_sort_one(c, ra, o, s, &g_last_launches);
+  if (e != cudaSuccess) return cuda_status(e);
   // Deliver the device-chosen final home into the caller's buffers.
-  rc = cuda_status(
-      launch_sort_deliver(bufs, reinterpret_cast<WahCtrl*>(ws + l.ctrl), n, d_sorted_values,
-                          d_rids, s, &g_last_launches));
-  return rc;
+  return cuda_status(launch_sort_deliver(c, d_sorted_values, d_rids, s, &g_last_launches));
 }
 
 int wah_build_sorted(const uint32_t* d_sorted_values, const uint32_t* d_rids, uint64_t n,
@@ -277,28 +276,24 @@ int wah_build_sorted(const uint32_t* d_sorted_values, const uint32_t* d_rids, ui
   if (!aligned16(d_sorted_values) || !aligned16(d_rids)) return WAH_EINVAL;
   const WsLayout l = ws_layout(n);
   if (workspace_bytes < l.total) return WAH_ENOMEM;
-  unsigned char* ws = static_cast<unsigned char*>(d_workspace);
-  WahCtrl* ctrl = reinterpret_cast<WahCtrl*>(ws + l.ctrl);
-  e = cudaMemsetAsync(ctrl, 0, sizeof(WahCtrl), s);
+  ColumnView c;
+  RangeArrays ra;
+  workspace_views(l, static_cast<unsigned char*>(d_workspace), n, &c, &ra);
+  c.input = d_sorted_values;
+  c.input_rids = d_rids;
+  c.fixed_sel = kSelInput;
+  c.keys = d_keys;
+  c.offsets = d_offsets;
+  c.index = d_index;
+  wah_output_caps(n, 0, &c.keys_cap, &c.index_cap);
+  c.counts = d_counts;
+  c.status = &d_counts->status;
+  c.passes = kDigits;
+  const LaunchOpts o = launch_opts(kDigits, nullptr);
+  if (o.sm_count <= 0) return WAH_ENODEV;
+  e = cudaMemsetAsync(c.ctrl, 0, sizeof(WahCtrl), s);
   if (e != cudaSuccess) return cuda_status(e);
-  BuildLaunch b;
-  b.events = nullptr;
-  b.src.keys[0] = d_sorted_values;
-  b.src.rids[0] = d_rids;
-  b.src.keys[1] = b.src.keys[2] = nullptr;
-  b.src.rids[1] = b.src.rids[2] = nullptr;
-  b.sel = 0;
-  b.n = n;
-  b.ctrl = ctrl;
-  b.range_counts = reinterpret_cast<uint32_t*>(ws + l.lb_build);
-  b.range_first = b.range_counts + kMaxRanges * 4;
-  b.sm_count = sm_count_current();
-  b.keys = d_keys;
-  b.offsets = d_offsets;
-  b.index = d_index;
-  wah_output_caps(n, 0, &b.keys_cap, &b.index_cap);
-  b.counts = d_counts;
-  return cuda_status(launch_build(b, s, &g_last_launches));
+  return cuda_status(launch_build_one(c, ra, o, s, &g_last_launches));
 }
 
 // ---------------------------------------------------------------------------

@@ -27,10 +27,6 @@ constexpr int kSortThreads = 256;
 constexpr int kMaxRanges = 1024;
 constexpr int kCountCtasPerRange = 2;
 
-struct RangeGeom {
-  uint64_t range_rows;  // rows per range, a multiple of the scatter tile
-  uint32_t ranges;      // number of ranges (<= kMaxRanges)
-};
 
 // Fused index build: 256 threads x 8 rows, blocked.
 constexpr int kBuildThreads = 256;
@@ -72,11 +68,6 @@ struct WahCtrl {
   uint32_t pad[2];
 };
 
-// Pointers of the three possible key/rid homes (input, A, B).
-struct SortBufs {
-  const uint32_t* keys[3];
-  const uint32_t* rids[3];  // rids[kSelInput] == nullptr: rid = row index
-};
 
 __host__ __device__ constexpr inline uint64_t ceil_div(uint64_t a, uint64_t b) {
   return (a + b - 1) / b;
@@ -261,44 +252,120 @@ inline void record_phase(cudaEvent_t* ev, int phase, bool end, cudaStream_t s) {
   if (ev) cudaEventRecord(ev[2 * phase + (end ? 1 : 0)], s);
 }
 
-// Host-side launchers (defined in the .cu files).
-struct SortLaunch {
-  const uint32_t* values;
-  uint64_t n;
-  int passes;  // digit passes to launch (1..4)
-  WahCtrl* ctrl;
-  uint32_t* range_hist;   // [kDigits][kMaxRanges][256] u32, zeroed per build
-  uint32_t* range_start;  // [kMaxRanges][256] u32
-  uint32_t* buf_keys[2];
-  uint32_t* buf_rids[2];
-  uint32_t* status;
-  int sm_count;
-  int sort_items;       // onesweep rows per thread (8, 12, 16, 20)
-  int sort_peers;       // peer masks: 0 ballots, 1 match.any, 2 half and half
-  cudaEvent_t* events;  // optional: [2*phase] before, [2*phase+1] after
-};
-
-cudaError_t launch_sort(const SortLaunch& a, cudaStream_t s, uint32_t* launches);
-cudaError_t launch_sort_deliver(const SortBufs& bufs, const WahCtrl* ctrl, uint64_t n,
-                                uint32_t* out_keys, uint32_t* out_rids, cudaStream_t s,
-                                uint32_t* launches);
-
-struct BuildLaunch {
-  SortBufs src;
-  int sel;  // -1: take WahCtrl::final_sel, else a fixed selector
+// ---------------------------------------------------------------------------
+// Columns and ranges as the kernels see them.
+//
+// Every kernel works on row ranges; a range lies inside one column.  A
+// geometry maps a range id to (column, rows [lo, hi)) and a column id to its
+// buffers.  OneColumn carries the single column of wah_build in the kernel
+// parameters; ManyColumns reads per-column and per-range tables from device
+// memory (wah_build_batched), so one launch of each kernel covers every
+// column of a batch.
+// ---------------------------------------------------------------------------
+struct ColumnView {
+  const uint32_t* input;       // the caller's values (selector kSelInput)
+  const uint32_t* input_rids;  // nullptr: rid = row index; else the caller's rids
+  uint32_t* keys_a;            // ping-pong homes of the sort (n rows each)
+  uint32_t* rids_a;
+  uint32_t* keys_b;
+  uint32_t* rids_b;
   uint64_t n;
   WahCtrl* ctrl;
-  uint32_t* range_counts;  // [kMaxRanges][4] words, keys, segments per range
-  uint32_t* range_first;   // [kMaxRanges][2] first word and key of each range
-  int sm_count;
-  uint32_t* keys;
+  uint32_t* keys;  // outputs
   uint32_t* offsets;
   uint32_t* index;
   uint64_t keys_cap;
   uint64_t index_cap;
-  wah_counts* counts;
-  cudaEvent_t* events;  // optional, phase kPhaseBuild
+  wah_counts* counts;  // build results (nullptr when only sorting)
+  uint32_t* status;    // device-side errors of this column
+  int32_t passes;      // digit passes its bound allows (1..4)
+  int32_t fixed_sel;   // >= 0: the build reads this home instead of final_sel
 };
-cudaError_t launch_build(const BuildLaunch& a, cudaStream_t s, uint32_t* launches);
+
+struct RangeView {
+  uint32_t col;
+  uint32_t pad;
+  uint64_t lo, hi;  // rows of the column
+};
+
+__host__ __device__ __forceinline__ const uint32_t* sel_keys(const ColumnView& c, int s) {
+  return s == kSelInput ? c.input : (s == kSelA ? c.keys_a : c.keys_b);
+}
+__host__ __device__ __forceinline__ const uint32_t* sel_rids(const ColumnView& c, int s) {
+  return s == kSelInput ? c.input_rids : (s == kSelA ? c.rids_a : c.rids_b);
+}
+
+struct OneColumn {
+  ColumnView c;
+  uint64_t range_rows;  // multiple of every tile size
+  uint32_t ranges;
+  __device__ __forceinline__ const ColumnView& col(uint32_t) const { return c; }
+  __device__ __forceinline__ RangeView range(uint32_t r) const {
+    RangeView v;
+    v.col = 0;
+    v.pad = 0;
+    const uint64_t lo = (uint64_t)r * range_rows;
+    v.lo = lo < c.n ? lo : c.n;
+    v.hi = lo + range_rows < c.n ? lo + range_rows : c.n;
+    return v;
+  }
+  __device__ __forceinline__ uint32_t first_range(uint32_t) const { return 0; }
+  __device__ __forceinline__ uint32_t end_range(uint32_t) const { return ranges; }
+};
+
+struct ManyColumns {
+  const ColumnView* cols;     // [ncols]
+  const RangeView* rngs;      // [ranges]; each column's ranges are contiguous
+  const uint32_t* col_first;  // [ncols]: first range of each column
+  const uint32_t* col_end;    // [ncols]: one past its last range
+  __device__ __forceinline__ ColumnView col(uint32_t c) const { return cols[c]; }
+  __device__ __forceinline__ RangeView range(uint32_t r) const { return rngs[r]; }
+  __device__ __forceinline__ uint32_t first_range(uint32_t c) const { return col_first[c]; }
+  __device__ __forceinline__ uint32_t end_range(uint32_t c) const { return col_end[c]; }
+};
+
+// Range bookkeeping arrays of one build (device memory).
+struct RangeArrays {
+  uint32_t* hist;    // [kDigits][max_ranges][256] digit counts per range, zeroed per build
+  uint32_t* start;   // [max_ranges][256] first output position per (range, bin)
+  uint32_t* counts;  // [max_ranges][4] words, keys, segments per range
+  uint32_t* first;   // [max_ranges][2] first word and key per range
+  uint32_t max_ranges;
+};
+
+// Tuning and instrumentation of one launch sequence.
+struct LaunchOpts {
+  int sort_items;       // radix tile rows per thread (8, 12, 16)
+  int sort_peers;       // peer masks: 0 ballots, 1 match.any, 2 half and half
+  int max_passes;       // digit passes launched (max over the columns)
+  int sm_count;
+  cudaEvent_t* events;  // optional: [2*phase] before, [2*phase+1] after
+};
+
+// Host-side launchers (defined in the .cu files).  The one-column forms
+// choose the range geometry themselves; the batched forms take it from the
+// plan (ranges, per-column tables).
+cudaError_t launch_sort_one(const ColumnView& c, const RangeArrays& ra, const LaunchOpts& o,
+                            cudaStream_t s, uint32_t* launches);
+cudaError_t launch_build_one(const ColumnView& c, const RangeArrays& ra, const LaunchOpts& o,
+                             cudaStream_t s, uint32_t* launches);
+cudaError_t launch_sort_many(const ManyColumns& g, uint32_t ncols, uint32_t ranges,
+                             const RangeArrays& ra, const LaunchOpts& o, cudaStream_t s,
+                             uint32_t* launches);
+cudaError_t launch_build_many(const ManyColumns& g, uint32_t ncols, uint32_t ranges,
+                              const RangeArrays& ra, const LaunchOpts& o, cudaStream_t s,
+                              uint32_t* launches);
+// Tile sizes the batched planner must respect (ranges are whole tiles except
+// a column's last).
+constexpr uint64_t kRangeQuantum = 4096;
+cudaError_t launch_sort_deliver(const ColumnView& c, uint32_t* out_keys, uint32_t* out_rids,
+                                cudaStream_t s, uint32_t* launches);
+
+// Shared host helpers (wah_api.cu).
+int passes_for_bound(uint32_t bound);
+int sm_count_current();
+int cuda_status(cudaError_t e);
+LaunchOpts launch_opts(int max_passes, cudaEvent_t* events);
+uint32_t* last_launches_slot();
 
 }  // namespace wah

@@ -67,19 +67,20 @@ __device__ __forceinline__ void count_row(uint32_t v, uint32_t c, uint32_t pv, u
   segs += h;
 }
 
+template <class G>
 __global__ void __launch_bounds__(kHistThreads)
-    k_build_count(SortBufs bufs, int sel, uint64_t n, RangeGeom g, const WahCtrl* ctrl,
-                  uint32_t* __restrict__ range_counts /* [ranges][4] */) {
-  const int s = sel >= 0 ? sel : ctrl->final_sel;
-  const uint32_t* __restrict__ sv = s == 0 ? bufs.keys[0] : (s == 1 ? bufs.keys[1] : bufs.keys[2]);
-  const uint32_t* __restrict__ sr = s == 0 ? bufs.rids[0] : (s == 1 ? bufs.rids[1] : bufs.rids[2]);
-  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    k_build_count(G g, uint32_t* __restrict__ range_counts /* [ranges][4] */) {
   const uint32_t c = blockIdx.x / kCountCtasPerRange, q = blockIdx.x % kCountCtasPerRange;
-  const uint64_t part = g.range_rows / kCountCtasPerRange;  // multiple of 4
-  uint64_t lo = (uint64_t)c * g.range_rows + q * part;
-  uint64_t hi = q + 1 == kCountCtasPerRange ? (uint64_t)(c + 1) * g.range_rows : lo + part;
-  lo = lo < n ? lo : n;
-  hi = hi < n ? hi : n;
+  const RangeView rv = g.range(c);
+  const ColumnView col = g.col(rv.col);
+  const int s = col.fixed_sel >= 0 ? col.fixed_sel : col.ctrl->final_sel;
+  const uint32_t* __restrict__ sv = sel_keys(col, s);
+  const uint32_t* __restrict__ sr = sel_rids(col, s);
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  // part q of the range (parts start on multiples of 4 rows: aligned loads)
+  const uint64_t part = ((rv.hi - rv.lo) / kCountCtasPerRange) & ~(uint64_t)3;
+  const uint64_t lo = rv.lo + q * part;
+  const uint64_t hi = q + 1 == kCountCtasPerRange ? rv.hi : lo + part;
 
   uint32_t words = 0, keys = 0, segs = 0;
   const uint64_t chunks = (hi - lo) / 128;  // 32 lanes x 4 rows
@@ -143,27 +144,31 @@ __global__ void __launch_bounds__(kHistThreads)
 constexpr int kBuildScanThreads = 1024;
 static_assert(kBuildScanThreads >= kMaxRanges, "one thread per range");
 
+// One CTA per column, one thread per range of the column (<= kMaxRanges).
+template <class G>
 __global__ void __launch_bounds__(kBuildScanThreads)
-    k_build_scan(uint32_t ranges, const uint32_t* __restrict__ range_counts,
-                 uint32_t* __restrict__ range_first /* [ranges][2] */, wah_counts* counts) {
+    k_build_scan(G g, const uint32_t* __restrict__ range_counts,
+                 uint32_t* __restrict__ range_first /* [ranges][2] */) {
   __shared__ uint64_t s_warp[kBuildScanThreads / 32 + 1];
-  const uint32_t c = threadIdx.x;
+  const ColumnView col = g.col(blockIdx.x);
+  const uint32_t r0 = g.first_range(blockIdx.x), r1 = g.end_range(blockIdx.x);
+  const uint32_t c = r0 + threadIdx.x;
   uint64_t x = 0;
   uint32_t segs = 0;
-  if (c < ranges) {
+  if (c < r1) {
     x = ((uint64_t)range_counts[c * 4 + 1] << 32) | range_counts[c * 4 + 0];
     segs = range_counts[c * 4 + 2];
   }
   uint64_t total;
   const uint64_t excl = block_exclusive_scan64<kBuildScanThreads>(x, &total, s_warp);
-  if (c < ranges) {
+  if (c < r1) {
     range_first[c * 2 + 0] = (uint32_t)(excl & 0xffffffffu);
     range_first[c * 2 + 1] = (uint32_t)(excl >> 32);
   }
-  if (segs) atomicAdd(&counts->merged, segs);
-  if (c == 0) {
-    counts->index_len = (uint32_t)(total & 0xffffffffu);
-    counts->keycnt = (uint32_t)(total >> 32);
+  if (segs) atomicAdd(&col.counts->merged, segs);
+  if (threadIdx.x == 0) {
+    col.counts->index_len = (uint32_t)(total & 0xffffffffu);
+    col.counts->keycnt = (uint32_t)(total >> 32);
   }
 }
 
@@ -179,21 +184,6 @@ struct EmitSmem {
   uint64_t warp_tmp[kBuildThreads / 32 + 1];
   uint64_t bar[2];
   int abort;
-};
-
-struct EmitArgs {
-  SortBufs bufs;
-  int sel;
-  uint64_t n;
-  RangeGeom g;
-  const WahCtrl* ctrl;
-  const uint32_t* range_first;
-  uint32_t* keys;
-  uint32_t* offsets;
-  uint32_t* index;
-  uint64_t keys_cap;
-  uint64_t index_cap;
-  uint32_t* status;
 };
 
 // A tile's window can come by bulk copy when all its rows exist and it does
@@ -212,23 +202,29 @@ __device__ __forceinline__ void fetch_window(uint32_t* wv, uint32_t* wr, uint64_
   if (sr) bulk_copy_g2s(wr, sr + base - kWinBehind, bytes, bar);
 }
 
-__global__ void __launch_bounds__(kBuildThreads, 3) k_build_emit(EmitArgs a) {
+template <class G>
+__global__ void __launch_bounds__(kBuildThreads, 3)
+    k_build_emit(G g, const uint32_t* __restrict__ range_first) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   EmitSmem& sm = *reinterpret_cast<EmitSmem*>(smem_raw);
-  const int s = a.sel >= 0 ? a.sel : a.ctrl->final_sel;
-  const uint32_t* __restrict__ sv =
-      s == 0 ? a.bufs.keys[0] : (s == 1 ? a.bufs.keys[1] : a.bufs.keys[2]);
-  const uint32_t* __restrict__ sr =
-      s == 0 ? a.bufs.rids[0] : (s == 1 ? a.bufs.rids[1] : a.bufs.rids[2]);
+  const RangeView rv = g.range(blockIdx.x);
+  const ColumnView col = g.col(rv.col);
+  const int s = col.fixed_sel >= 0 ? col.fixed_sel : col.ctrl->final_sel;
+  const uint32_t* __restrict__ sv = sel_keys(col, s);
+  const uint32_t* __restrict__ sr = sel_rids(col, s);
+  uint32_t* __restrict__ out_index = col.index;
+  uint32_t* __restrict__ out_keys = col.keys;
+  uint32_t* __restrict__ out_offsets = col.offsets;
+  const uint64_t keys_cap = col.keys_cap, index_cap = col.index_cap;
+  uint32_t* status = col.status;
 
   const uint32_t tid = threadIdx.x;
-  const uint64_t n = a.n;
-  const uint64_t lo = (uint64_t)blockIdx.x * a.g.range_rows;
-  if (lo >= n) return;
-  const uint64_t hi = lo + a.g.range_rows < n ? lo + a.g.range_rows : n;
+  const uint64_t n = col.n;
+  const uint64_t lo = rv.lo, hi = rv.hi;
+  if (lo >= hi) return;
   const uint32_t ntiles = (uint32_t)ceil_div(hi - lo, kBuildTile);
-  uint32_t run_w = a.range_first[blockIdx.x * 2 + 0];  // words before this tile
-  uint32_t run_k = a.range_first[blockIdx.x * 2 + 1];  // keys before this tile
+  uint32_t run_w = range_first[blockIdx.x * 2 + 0];  // words before this tile
+  uint32_t run_k = range_first[blockIdx.x * 2 + 1];  // keys before this tile
 
   if (tid == 0) {
     mbar_init(&sm.bar[0], 1);
@@ -261,7 +257,7 @@ __global__ void __launch_bounds__(kBuildThreads, 3) k_build_emit(EmitArgs a) {
       const bool ok = mbar_wait_bounded(&sm.bar[cur], (phase_bits >> cur) & 1u);
       phase_bits ^= 1u << cur;
       if (!ok) {
-        set_status(a.status, WAH_ETIMEOUT);
+        set_status(status, WAH_ETIMEOUT);
         sm.abort = 1;
       }
       if (!sr) {  // identity row ids: the bulk copy brought values only
@@ -371,21 +367,21 @@ __global__ void __launch_bounds__(kBuildThreads, 3) k_build_emit(EmitArgs a) {
       bool overflow = false;
       for (uint32_t k = tid; k < tw; k += kBuildThreads) {
         const uint64_t pos = (uint64_t)run_w + k;
-        if (pos < a.index_cap)
-          a.index[pos] = sm.words[skew(k)];
+        if (pos < index_cap)
+          out_index[pos] = sm.words[skew(k)];
         else
           overflow = true;
       }
       for (uint32_t k = tid; k < tk; k += kBuildThreads) {
         const uint64_t pos = (uint64_t)run_k + k;
-        if (pos < a.keys_cap) {
-          a.keys[pos] = sm.keys[skew(k)];
-          a.offsets[pos] = sm.offs[skew(k)];
+        if (pos < keys_cap) {
+          out_keys[pos] = sm.keys[skew(k)];
+          out_offsets[pos] = sm.offs[skew(k)];
         } else {
           overflow = true;
         }
       }
-      if (overflow) set_status(a.status, WAH_EOVERFLOW);
+      if (overflow) set_status(status, WAH_EOVERFLOW);
     }
     run_w += tw;
     run_k += tk;
@@ -396,45 +392,48 @@ __global__ void __launch_bounds__(kBuildThreads, 3) k_build_emit(EmitArgs a) {
 // ---------------------------------------------------------------------------
 // Host side.
 // ---------------------------------------------------------------------------
-cudaError_t launch_build(const BuildLaunch& a, cudaStream_t s, uint32_t* launches) {
+template <class G>
+cudaError_t launch_build_t(const G& g, uint32_t ncols, uint32_t ranges, const RangeArrays& ra,
+                           const LaunchOpts& o, cudaStream_t s, uint32_t* launches) {
   const size_t smem = sizeof(EmitSmem);
-  cudaError_t err =
-      cudaFuncSetAttribute(k_build_emit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t err = cudaFuncSetAttribute(k_build_emit<G>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (err != cudaSuccess) return err;
-  int per_sm = 0;
-  err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_build_emit, kBuildThreads, smem);
+  err = cudaMemsetAsync(ra.counts, 0, (size_t)ra.max_ranges * 4 * sizeof(uint32_t), s);
   if (err != cudaSuccess) return err;
-  uint64_t want = (uint64_t)std::max(a.sm_count, 1) * std::max(per_sm, 1);
-  if (want > kMaxRanges) want = kMaxRanges;
-  RangeGeom g;
-  g.range_rows =
-      std::max<uint64_t>(ceil_div(ceil_div(a.n, want), kBuildTile) * kBuildTile, kBuildTile);
-  g.ranges = (uint32_t)std::max<uint64_t>(ceil_div(a.n, g.range_rows), 1);
-
-  err = cudaMemsetAsync(a.range_counts, 0, (size_t)kMaxRanges * 4 * sizeof(uint32_t), s);
-  if (err != cudaSuccess) return err;
-  record_phase(a.events, kPhaseBuild, false, s);
-  k_build_count<<<g.ranges * kCountCtasPerRange, kHistThreads, 0, s>>>(a.src, a.sel, a.n, g,
-                                                                       a.ctrl, a.range_counts);
-  k_build_scan<<<1, kBuildScanThreads, 0, s>>>(g.ranges, a.range_counts, a.range_first,
-                                               a.counts);
-  EmitArgs e;
-  e.bufs = a.src;
-  e.sel = a.sel;
-  e.n = a.n;
-  e.g = g;
-  e.ctrl = a.ctrl;
-  e.range_first = a.range_first;
-  e.keys = a.keys;
-  e.offsets = a.offsets;
-  e.index = a.index;
-  e.keys_cap = a.keys_cap;
-  e.index_cap = a.index_cap;
-  e.status = &a.counts->status;
-  k_build_emit<<<g.ranges, kBuildThreads, smem, s>>>(e);
-  record_phase(a.events, kPhaseBuild, true, s);
+  record_phase(o.events, kPhaseBuild, false, s);
+  k_build_count<G><<<ranges * kCountCtasPerRange, kHistThreads, 0, s>>>(g, ra.counts);
+  k_build_scan<G><<<ncols, kBuildScanThreads, 0, s>>>(g, ra.counts, ra.first);
+  k_build_emit<G><<<ranges, kBuildThreads, smem, s>>>(g, ra.first);
+  record_phase(o.events, kPhaseBuild, true, s);
   *launches += 3;
   return cudaGetLastError();
+}
+
+cudaError_t launch_build_one(const ColumnView& c, const RangeArrays& ra, const LaunchOpts& o,
+                             cudaStream_t s, uint32_t* launches) {
+  int per_sm = 0;
+  cudaError_t err = cudaFuncSetAttribute(k_build_emit<OneColumn>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)sizeof(EmitSmem));
+  if (err != cudaSuccess) return err;
+  err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_build_emit<OneColumn>,
+                                                      kBuildThreads, sizeof(EmitSmem));
+  if (err != cudaSuccess) return err;
+  uint64_t want = (uint64_t)std::max(o.sm_count, 1) * std::max(per_sm, 1);
+  if (want > ra.max_ranges) want = ra.max_ranges;
+  OneColumn g;
+  g.c = c;
+  g.range_rows =
+      std::max<uint64_t>(ceil_div(ceil_div(c.n, want), kBuildTile) * kBuildTile, kBuildTile);
+  g.ranges = (uint32_t)std::max<uint64_t>(ceil_div(c.n, g.range_rows), 1);
+  return launch_build_t<OneColumn>(g, 1, g.ranges, ra, o, s, launches);
+}
+
+cudaError_t launch_build_many(const ManyColumns& g, uint32_t ncols, uint32_t ranges,
+                              const RangeArrays& ra, const LaunchOpts& o, cudaStream_t s,
+                              uint32_t* launches) {
+  return launch_build_t<ManyColumns>(g, ncols, ranges, ra, o, s, launches);
 }
 
 }  // namespace wah

@@ -105,73 +105,78 @@ __device__ __forceinline__ uint32_t histogram_range(const uint32_t* __restrict__
   return __reduce_or_sync(0xffffffffu, acc_or);
 }
 
-// Sub-range q of range c: the rows one histogram CTA covers.
-__device__ __forceinline__ void sub_range(const RangeGeom& g, uint64_t n, uint32_t cta,
-                                          uint64_t* lo, uint64_t* hi) {
-  const uint32_t c = cta / kCountCtasPerRange, q = cta % kCountCtasPerRange;
-  const uint64_t part = g.range_rows / kCountCtasPerRange;  // multiple of 4
-  const uint64_t a = (uint64_t)c * g.range_rows + q * part;
-  const uint64_t b = q + 1 == kCountCtasPerRange ? (uint64_t)(c + 1) * g.range_rows : a + part;
-  *lo = a < n ? a : n;
-  *hi = b < n ? b : n;
+// Part q of a range: the rows one counting CTA covers (parts start on
+// multiples of 4 rows, so 16-byte loads stay aligned).
+__device__ __forceinline__ void sub_range(const RangeView& rv, uint32_t q, uint64_t* lo,
+                                          uint64_t* hi) {
+  const uint64_t part = ((rv.hi - rv.lo) / kCountCtasPerRange) & ~(uint64_t)3;
+  *lo = rv.lo + q * part;
+  *hi = q + 1 == kCountCtasPerRange ? rv.hi : *lo + part;
 }
 
-template <int DIGITS>
+template <int DIGITS, class G>
 __global__ void __launch_bounds__(kHistThreads)
-    k_digit_histogram(const uint32_t* __restrict__ keys, uint64_t n, RangeGeom g, WahCtrl* ctrl,
-                      uint32_t* __restrict__ range_hist0) {
+    k_digit_histogram(G g, uint32_t* __restrict__ range_hist0) {
   __shared__ uint32_t s_h[kHistWarps][DIGITS][kRadix];
   for (int i = threadIdx.x; i < kHistWarps * DIGITS * kRadix; i += kHistThreads)
     (&s_h[0][0][0])[i] = 0;
   __syncthreads();
+  const uint32_t r = blockIdx.x / kCountCtasPerRange;
+  const RangeView rv = g.range(r);
+  const ColumnView c = g.col(rv.col);
   uint64_t lo, hi;
-  sub_range(g, n, blockIdx.x, &lo, &hi);
-  const uint32_t acc_or = histogram_range<DIGITS>(keys, lo, hi, 0, s_h);
-  if ((threadIdx.x & 31) == 0 && acc_or) atomicOr(&ctrl->key_or, acc_or);
+  sub_range(rv, blockIdx.x % kCountCtasPerRange, &lo, &hi);
+  const uint32_t acc_or = histogram_range<DIGITS>(c.input, lo, hi, 0, s_h);
+  if ((threadIdx.x & 31) == 0 && acc_or) atomicOr(&c.ctrl->key_or, acc_or);
   __syncthreads();
-  const uint32_t c = blockIdx.x / kCountCtasPerRange;
   for (int j = threadIdx.x; j < DIGITS * kRadix; j += kHistThreads) {
     uint32_t s = 0;
 #pragma unroll
     for (int w = 0; w < kHistWarps; ++w) s += (&s_h[w][0][0])[j];
     if (s) {
-      atomicAdd(&(&ctrl->hist[0][0])[j], s);
-      if (j < kRadix) atomicAdd(&range_hist0[(uint64_t)c * kRadix + j], s);
+      atomicAdd(&(&c.ctrl->hist[0][0])[j], s);
+      if (j < kRadix) atomicAdd(&range_hist0[(uint64_t)r * kRadix + j], s);
     }
   }
 }
 
 // Per-range histogram of digit `pass` over the current order of the keys.
+template <class G>
 __global__ void __launch_bounds__(kHistThreads)
-    k_range_count(const uint32_t* input, const uint32_t* keys_a, const uint32_t* keys_b,
-                  uint64_t n, RangeGeom g, int pass, const WahCtrl* ctrl,
-                  uint32_t* __restrict__ range_hist) {
-  const int src = ctrl->pass_src[pass];
+    k_range_count(G g, int pass, uint32_t* __restrict__ range_hist) {
+  const uint32_t r = blockIdx.x / kCountCtasPerRange;
+  const RangeView rv = g.range(r);
+  const ColumnView c = g.col(rv.col);
+  const int src = c.ctrl->pass_src[pass];
   if (src < 0) return;
-  const uint32_t* keys = src == kSelInput ? input : (src == kSelA ? keys_a : keys_b);
+  const uint32_t* keys = sel_keys(c, src);
   __shared__ uint32_t s_h[kHistWarps][1][kRadix];
   for (int i = threadIdx.x; i < kHistWarps * kRadix; i += kHistThreads) (&s_h[0][0][0])[i] = 0;
   __syncthreads();
   uint64_t lo, hi;
-  sub_range(g, n, blockIdx.x, &lo, &hi);
+  sub_range(rv, blockIdx.x % kCountCtasPerRange, &lo, &hi);
   histogram_range<1>(keys, lo, hi, pass, s_h);
   __syncthreads();
-  const uint32_t c = blockIdx.x / kCountCtasPerRange;
   for (int j = threadIdx.x; j < kRadix; j += kHistThreads) {
     uint32_t s = 0;
 #pragma unroll
     for (int w = 0; w < kHistWarps; ++w) s += s_h[w][0][j];
-    if (s) atomicAdd(&range_hist[(uint64_t)c * kRadix + j], s);
+    if (s) atomicAdd(&range_hist[(uint64_t)r * kRadix + j], s);
   }
 }
 
 // ---------------------------------------------------------------------------
 // Pass plan: bin offsets per digit, trivial digits skipped, ping-pong homes.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kRadix)
-    k_sort_plan(WahCtrl* ctrl, uint64_t n, int passes, uint32_t* status) {
+template <class G>
+__global__ void __launch_bounds__(kRadix) k_sort_plan(G g) {
   __shared__ uint32_t s_warp[kRadix / 32 + 1];
   __shared__ int s_active[kDigits];
+  const ColumnView c = g.col(blockIdx.x);
+  WahCtrl* ctrl = c.ctrl;
+  const uint64_t n = c.n;
+  const int passes = c.passes;
+  uint32_t* status = c.status;
   const int b = threadIdx.x;
   for (int p = 0; p < passes; ++p) {
     const uint32_t h = ctrl->hist[p][b];
@@ -202,15 +207,18 @@ __global__ void __launch_bounds__(kRadix)
   }
 }
 
-// Start of every (range, bin) for one pass.
+// Start of every (range, bin) of one column for one pass.
+template <class G>
 __global__ void __launch_bounds__(kRadix)
-    k_range_scan(const WahCtrl* ctrl, int pass, uint32_t ranges,
-                 const uint32_t* __restrict__ range_hist, uint32_t* __restrict__ range_start) {
-  if (ctrl->pass_src[pass] < 0) return;
+    k_range_scan(G g, int pass, const uint32_t* __restrict__ range_hist,
+                 uint32_t* __restrict__ range_start) {
+  const ColumnView col = g.col(blockIdx.x);
+  if (col.ctrl->pass_src[pass] < 0) return;
   const uint32_t b = threadIdx.x;
-  uint32_t run = ctrl->bin_off[pass][b];
-  uint32_t c = 0;
-  for (; c + 8 <= ranges; c += 8) {
+  uint32_t run = col.ctrl->bin_off[pass][b];
+  uint32_t c = g.first_range(blockIdx.x);
+  const uint32_t end = g.end_range(blockIdx.x);
+  for (; c + 8 <= end; c += 8) {
     uint32_t h[8];
 #pragma unroll
     for (int u = 0; u < 8; ++u) h[u] = range_hist[(uint64_t)(c + u) * kRadix + b];
@@ -220,7 +228,7 @@ __global__ void __launch_bounds__(kRadix)
       run += h[u];
     }
   }
-  for (; c < ranges; ++c) {
+  for (; c < end; ++c) {
     range_start[(uint64_t)c * kRadix + b] = run;
     run += range_hist[(uint64_t)c * kRadix + b];
   }
@@ -260,20 +268,6 @@ struct ScatterSmem {
   int abort;
 };
 
-struct ScatterArgs {
-  const uint32_t* input;  // selector kSelInput (rid = row index)
-  uint32_t* keys_a;
-  uint32_t* rids_a;
-  uint32_t* keys_b;
-  uint32_t* rids_b;
-  uint64_t n;
-  RangeGeom g;
-  int pass;
-  const WahCtrl* ctrl;
-  const uint32_t* range_start;  // [ranges][256]
-  uint32_t* status;
-};
-
 // Lanes of the warp holding the same 8-bit digit as this lane: eight ballots
 // (ALU pipe) or __match_any_sync (MIO pipe).
 template <bool BALLOT>
@@ -305,29 +299,32 @@ __device__ __forceinline__ void fetch_tile(uint32_t* dst_k, uint32_t* dst_r, uin
 
 // PEERS: 0 all items by ballots, 1 all by match.any, 2 the first half by
 // match.any and the second by ballots (the two pipes work in parallel).
-template <int ITEMS, int PEERS>
-__global__ void __launch_bounds__(kSortThreads, 2) k_radix_scatter(ScatterArgs a) {
+template <int ITEMS, int PEERS, class G>
+__global__ void __launch_bounds__(kSortThreads, 2)
+    k_radix_scatter(G g, int pass, const uint32_t* __restrict__ range_start) {
   constexpr uint32_t TILE = kSortThreads * ITEMS;
   constexpr int HALF = ITEMS / 2;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   ScatterSmem<ITEMS>& sm = *reinterpret_cast<ScatterSmem<ITEMS>*>(smem_raw);
 
-  const int src = a.ctrl->pass_src[a.pass];
+  const RangeView rv = g.range(blockIdx.x);
+  const ColumnView col = g.col(rv.col);
+  const int src = col.ctrl->pass_src[pass];
   if (src < 0) return;  // trivial digit: every row in one bin, order unchanged
-  const int dst = a.ctrl->pass_dst[a.pass];
-  const uint32_t* kin = src == kSelInput ? a.input : (src == kSelA ? a.keys_a : a.keys_b);
-  const uint32_t* rin = src == kSelInput ? nullptr : (src == kSelA ? a.rids_a : a.rids_b);
-  uint32_t* __restrict__ kout = dst == kSelA ? a.keys_a : a.keys_b;
-  uint32_t* __restrict__ rout = dst == kSelA ? a.rids_a : a.rids_b;
+  const int dst = col.ctrl->pass_dst[pass];
+  const uint32_t* kin = sel_keys(col, src);
+  const uint32_t* rin = sel_rids(col, src);
+  uint32_t* __restrict__ kout = const_cast<uint32_t*>(sel_keys(col, dst));
+  uint32_t* __restrict__ rout = const_cast<uint32_t*>(sel_rids(col, dst));
+  uint32_t* status = col.status;
 
   const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const uint32_t shift = a.pass * kRadixBits;
-  const uint64_t lo = (uint64_t)blockIdx.x * a.g.range_rows;
-  if (lo >= a.n) return;
-  const uint64_t hi = lo + a.g.range_rows < a.n ? lo + a.g.range_rows : a.n;
+  const uint32_t shift = pass * kRadixBits;
+  const uint64_t lo = rv.lo, hi = rv.hi;
+  if (lo >= hi) return;
   const uint32_t ntiles = (uint32_t)ceil_div(hi - lo, TILE);
 
-  sm.run_off[tid] = a.range_start[(uint64_t)blockIdx.x * kRadix + tid];
+  sm.run_off[tid] = range_start[(uint64_t)blockIdx.x * kRadix + tid];
   if (tid == 0) {
     mbar_init(&sm.bar[0], 1);
     mbar_init(&sm.bar[1], 1);
@@ -366,7 +363,7 @@ __global__ void __launch_bounds__(kSortThreads, 2) k_radix_scatter(ScatterArgs a
       const bool ok = mbar_wait_bounded(&sm.bar[cur], (phase_bits >> cur) & 1u);
       phase_bits ^= 1u << cur;
       if (!ok) {
-        set_status(a.status, WAH_ETIMEOUT);
+        set_status(status, WAH_ETIMEOUT);
         sm.abort = 1;
       }
       const uint32_t* kp = sm.in_keys[cur] + row0;
@@ -448,7 +445,7 @@ __global__ void __launch_bounds__(kSortThreads, 2) k_radix_scatter(ScatterArgs a
     __syncthreads();
 
     if (!sm.abort) {
-      const uint32_t n32 = (uint32_t)a.n;
+      const uint32_t n32 = (uint32_t)col.n;
 #pragma unroll 4
       for (int it = 0; it < ITEMS; ++it) {
         const uint32_t k = it * kSortThreads + tid;
@@ -459,7 +456,7 @@ __global__ void __launch_bounds__(kSortThreads, 2) k_radix_scatter(ScatterArgs a
             kout[g] = kk;
             rout[g] = sm.out_rids[k];
           } else {
-            set_status(a.status, WAH_ETIMEOUT);
+            set_status(status, WAH_ETIMEOUT);
           }
         }
       }
@@ -473,139 +470,137 @@ __global__ void __launch_bounds__(kSortThreads, 2) k_radix_scatter(ScatterArgs a
 // ---------------------------------------------------------------------------
 // Compiled tile shapes of the scatter pass; sort_items selects one, the
 // autotuner measures them.
+template <class G>
 struct SortVariant {
   int items;
-  void (*fn)(ScatterArgs);
+  void (*fn)(G, int, const uint32_t*);
   size_t smem;
 };
 
-template <int PEERS>
-SortVariant sort_variant_peers(int items) {
+template <int PEERS, class G>
+SortVariant<G> sort_variant_peers(int items) {
   switch (items) {
-    case 8: return {8, k_radix_scatter<8, PEERS>, sizeof(ScatterSmem<8>)};
-    case 12: return {12, k_radix_scatter<12, PEERS>, sizeof(ScatterSmem<12>)};
-    default: return {16, k_radix_scatter<16, PEERS>, sizeof(ScatterSmem<16>)};
+    case 8: return {8, k_radix_scatter<8, PEERS, G>, sizeof(ScatterSmem<8>)};
+    case 12: return {12, k_radix_scatter<12, PEERS, G>, sizeof(ScatterSmem<12>)};
+    default: return {16, k_radix_scatter<16, PEERS, G>, sizeof(ScatterSmem<16>)};
   }
 }
 
-SortVariant sort_variant(int items, int peers) {
-  if (peers == 1) return sort_variant_peers<1>(items);
-  if (peers == 2) return sort_variant_peers<2>(items);
-  return sort_variant_peers<0>(items);
+template <class G>
+SortVariant<G> sort_variant(int items, int peers) {
+  if (peers == 1) return sort_variant_peers<1, G>(items);
+  if (peers == 2) return sort_variant_peers<2, G>(items);
+  return sort_variant_peers<0, G>(items);
 }
 
-// Equal ranges of whole tiles, one per resident scatter CTA.
-RangeGeom range_geometry(uint64_t n, int resident_ctas, int items) {
-  const uint64_t tile = (uint64_t)kSortThreads * items;
-  uint64_t want = (uint64_t)std::max(resident_ctas, 1);
-  if (want > kMaxRanges) want = kMaxRanges;
-  RangeGeom g;
-  g.range_rows = std::max<uint64_t>(ceil_div(ceil_div(n, want), tile) * tile, tile);
-  g.ranges = (uint32_t)std::max<uint64_t>(ceil_div(n, g.range_rows), 1);
-  return g;
-}
-
-cudaError_t launch_sort(const SortLaunch& a, cudaStream_t s, uint32_t* launches) {
-  const uint64_t n = a.n;
-  const SortVariant v = sort_variant(a.sort_items, a.sort_peers);
+template <class G>
+cudaError_t scatter_variant(const LaunchOpts& o, SortVariant<G>* v, int* per_sm) {
+  *v = sort_variant<G>(o.sort_items, o.sort_peers);
   cudaError_t err =
-      cudaFuncSetAttribute(v.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)v.smem);
+      cudaFuncSetAttribute(v->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)v->smem);
   if (err != cudaSuccess) return err;
-  int per_sm = 0;
-  err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, v.fn, kSortThreads, v.smem);
-  if (err != cudaSuccess) return err;
-  const RangeGeom g = range_geometry(n, a.sm_count * std::max(per_sm, 1), v.items);
-  const unsigned count_grid = g.ranges * kCountCtasPerRange;
-  err = cudaMemsetAsync(a.range_hist, 0, (size_t)kDigits * kMaxRanges * kRadix * 4, s);
-  if (err != cudaSuccess) return err;
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, v->fn, kSortThreads, v->smem);
+}
 
-  record_phase(a.events, kPhaseHist, false, s);
-  switch (a.passes) {
-    case 1:
-      k_digit_histogram<1><<<count_grid, kHistThreads, 0, s>>>(a.values, n, g, a.ctrl,
-                                                               a.range_hist);
-      break;
-    case 2:
-      k_digit_histogram<2><<<count_grid, kHistThreads, 0, s>>>(a.values, n, g, a.ctrl,
-                                                               a.range_hist);
-      break;
-    case 3:
-      k_digit_histogram<3><<<count_grid, kHistThreads, 0, s>>>(a.values, n, g, a.ctrl,
-                                                               a.range_hist);
-      break;
-    default:
-      k_digit_histogram<4><<<count_grid, kHistThreads, 0, s>>>(a.values, n, g, a.ctrl,
-                                                               a.range_hist);
-      break;
+// The launch sequence over any geometry: histogram, plan, then per digit
+// pass (count,) scan and scatter.
+template <class G>
+cudaError_t launch_sort_t(const G& g, uint32_t ncols, uint32_t ranges, const RangeArrays& ra,
+                          const LaunchOpts& o, const SortVariant<G>& v, cudaStream_t s,
+                          uint32_t* launches) {
+  const unsigned count_grid = ranges * kCountCtasPerRange;
+  cudaError_t err =
+      cudaMemsetAsync(ra.hist, 0, (size_t)kDigits * ra.max_ranges * kRadix * 4, s);
+  if (err != cudaSuccess) return err;
+  record_phase(o.events, kPhaseHist, false, s);
+  switch (o.max_passes) {
+    case 1: k_digit_histogram<1, G><<<count_grid, kHistThreads, 0, s>>>(g, ra.hist); break;
+    case 2: k_digit_histogram<2, G><<<count_grid, kHistThreads, 0, s>>>(g, ra.hist); break;
+    case 3: k_digit_histogram<3, G><<<count_grid, kHistThreads, 0, s>>>(g, ra.hist); break;
+    default: k_digit_histogram<4, G><<<count_grid, kHistThreads, 0, s>>>(g, ra.hist); break;
   }
-  record_phase(a.events, kPhaseHist, true, s);
+  record_phase(o.events, kPhaseHist, true, s);
   ++*launches;
-  record_phase(a.events, kPhasePlan, false, s);
-  k_sort_plan<<<1, kRadix, 0, s>>>(a.ctrl, n, a.passes, a.status);
-  record_phase(a.events, kPhasePlan, true, s);
+  record_phase(o.events, kPhasePlan, false, s);
+  k_sort_plan<G><<<ncols, kRadix, 0, s>>>(g);
+  record_phase(o.events, kPhasePlan, true, s);
   ++*launches;
   err = cudaGetLastError();
   if (err != cudaSuccess) return err;
-
-  ScatterArgs sa;
-  sa.input = a.values;
-  sa.keys_a = a.buf_keys[0];
-  sa.rids_a = a.buf_rids[0];
-  sa.keys_b = a.buf_keys[1];
-  sa.rids_b = a.buf_rids[1];
-  sa.n = n;
-  sa.g = g;
-  sa.ctrl = a.ctrl;
-  sa.range_start = a.range_start;
-  sa.status = a.status;
   for (int p = 0; p < kDigits; ++p) {
-    if (p >= a.passes) {  // not launched: empty span keeps every event valid
-      record_phase(a.events, kPhasePass0 + p, false, s);
-      record_phase(a.events, kPhasePass0 + p, true, s);
+    if (p >= o.max_passes) {  // not launched: empty span keeps every event valid
+      record_phase(o.events, kPhasePass0 + p, false, s);
+      record_phase(o.events, kPhasePass0 + p, true, s);
       continue;
     }
-    uint32_t* rh = a.range_hist + (size_t)p * kMaxRanges * kRadix;
-    record_phase(a.events, kPhasePass0 + p, false, s);
+    uint32_t* rh = ra.hist + (size_t)p * ra.max_ranges * kRadix;
+    record_phase(o.events, kPhasePass0 + p, false, s);
     if (p > 0) {
-      k_range_count<<<count_grid, kHistThreads, 0, s>>>(a.values, a.buf_keys[0], a.buf_keys[1],
-                                                        n, g, p, a.ctrl, rh);
+      k_range_count<G><<<count_grid, kHistThreads, 0, s>>>(g, p, rh);
       ++*launches;
     }
-    k_range_scan<<<1, kRadix, 0, s>>>(a.ctrl, p, g.ranges, rh, a.range_start);
+    k_range_scan<G><<<ncols, kRadix, 0, s>>>(g, p, rh, ra.start);
     ++*launches;
-    sa.pass = p;
-    v.fn<<<g.ranges, kSortThreads, v.smem, s>>>(sa);
+    v.fn<<<ranges, kSortThreads, v.smem, s>>>(g, p, ra.start);
     ++*launches;
-    record_phase(a.events, kPhasePass0 + p, true, s);
+    record_phase(o.events, kPhasePass0 + p, true, s);
     err = cudaGetLastError();
     if (err != cudaSuccess) return err;
   }
   return cudaSuccess;
 }
 
+cudaError_t launch_sort_one(const ColumnView& c, const RangeArrays& ra, const LaunchOpts& o,
+                            cudaStream_t s, uint32_t* launches) {
+  SortVariant<OneColumn> v;
+  int per_sm = 0;
+  cudaError_t err = scatter_variant<OneColumn>(o, &v, &per_sm);
+  if (err != cudaSuccess) return err;
+  // equal ranges of whole tiles (multiples of every tile size), one per
+  // resident scatter CTA
+  uint64_t want = (uint64_t)std::max(o.sm_count, 1) * std::max(per_sm, 1);
+  if (want > ra.max_ranges) want = ra.max_ranges;
+  const uint64_t tile = (uint64_t)kSortThreads * v.items;
+  const uint64_t quantum = std::max<uint64_t>(tile, kRangeQuantum);
+  OneColumn g;
+  g.c = c;
+  g.range_rows = std::max<uint64_t>(ceil_div(ceil_div(c.n, want), quantum) * quantum, quantum);
+  g.ranges = (uint32_t)std::max<uint64_t>(ceil_div(c.n, g.range_rows), 1);
+  return launch_sort_t<OneColumn>(g, 1, g.ranges, ra, o, v, s, launches);
+}
+
+cudaError_t launch_sort_many(const ManyColumns& g, uint32_t ncols, uint32_t ranges,
+                             const RangeArrays& ra, const LaunchOpts& o, cudaStream_t s,
+                             uint32_t* launches) {
+  SortVariant<ManyColumns> v;
+  int per_sm = 0;
+  cudaError_t err = scatter_variant<ManyColumns>(o, &v, &per_sm);
+  if (err != cudaSuccess) return err;
+  return launch_sort_t<ManyColumns>(g, ncols, ranges, ra, o, v, s, launches);
+}
+
 // Copies the sorted stream from its device-chosen home into caller buffers
 // (rid = row index when no pass ran: all values equal, or n == 1).
-__global__ void k_sort_deliver(SortBufs bufs, const WahCtrl* ctrl, uint64_t n,
-                               uint32_t* __restrict__ out_keys, uint32_t* __restrict__ out_rids) {
-  const int sel = ctrl->final_sel;
-  const uint32_t* __restrict__ k = sel == 0 ? bufs.keys[0] : (sel == 1 ? bufs.keys[1] : bufs.keys[2]);
-  const uint32_t* __restrict__ r = sel == 0 ? bufs.rids[0] : (sel == 1 ? bufs.rids[1] : bufs.rids[2]);
+__global__ void k_sort_deliver(ColumnView c, uint32_t* __restrict__ out_keys,
+                               uint32_t* __restrict__ out_rids) {
+  const int sel = c.ctrl->final_sel;
+  const uint32_t* __restrict__ k = sel_keys(c, sel);
+  const uint32_t* __restrict__ r = sel_rids(c, sel);
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < c.n; i += stride) {
     out_keys[i] = k[i];
     out_rids[i] = r ? r[i] : (uint32_t)i;
   }
 }
 
-cudaError_t launch_sort_deliver(const SortBufs& bufs, const WahCtrl* ctrl, uint64_t n,
-                                uint32_t* out_keys, uint32_t* out_rids, cudaStream_t s,
-                                uint32_t* launches) {
+cudaError_t launch_sort_deliver(const ColumnView& c, uint32_t* out_keys, uint32_t* out_rids,
+                                cudaStream_t s, uint32_t* launches) {
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const uint64_t want = ceil_div(n, 256), cap = (uint64_t)(sms > 0 ? sms : 1) * 8;
+  const uint64_t want = ceil_div(c.n, 256), cap = (uint64_t)(sms > 0 ? sms : 1) * 8;
   const int grid = (int)(want < cap ? want : cap);
-  k_sort_deliver<<<grid, 256, 0, s>>>(bufs, ctrl, n, out_keys, out_rids);
+  k_sort_deliver<<<grid, 256, 0, s>>>(c, out_keys, out_rids);
   ++*launches;
   return cudaGetLastError();
 }
