@@ -56,6 +56,12 @@ def parse():
     ap.add_argument("--card", type=int, default=65536, help="values uniform in [0, card)")
     ap.add_argument("--seed", type=int, default=20170101)
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-skewed", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--batch-cols", type=int, default=4096)
+    ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--serve-requests", type=int, default=20000)
+    ap.add_argument("--serve-budget-gb", type=int, default=64)
     ap.add_argument("--pipe-depth", type=int, default=3,
                     help="builds in flight in the end-to-end leg")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -134,6 +140,170 @@ class ClockSampler:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx,
                 "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def time_events(fn, steps, torch, stream):
+    """Mean ms of fn() over steps, CUDA events on `stream`."""
+    a = torch.cuda.Event(enable_timing=True)
+    b = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    a.record(stream)
+    for _ in range(steps):
+        fn()
+    b.record(stream)
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / steps
+
+
+def gen_skewed(kind: str, n: int, seed: int, torch, dev):
+    """Seeded device columns of the skewed / clustered workloads."""
+    g = torch.Generator(device=dev)
+    g.manual_seed(seed)
+    if kind == "zipf1.1":
+        w = 1.0 / np.arange(1, 65537, dtype=np.float64) ** 1.1
+        cdf = torch.from_numpy(np.cumsum(w) / w.sum()).to(dev)
+        u = torch.rand(n, generator=g, device=dev, dtype=torch.float64)
+        return torch.searchsorted(cdf, u).clamp_(max=65535).to(torch.int32)
+    if kind == "distinct16":
+        return torch.randint(0, 16, (n,), generator=g, device=dev, dtype=torch.int32)
+    if kind == "runs1000":
+        rng = np.random.default_rng(seed)
+        runs = rng.geometric(1 / 1000, size=n // 1000 * 2 + 16)
+        cum = np.cumsum(runs)
+        m = int(np.searchsorted(cum, n)) + 1
+        runs = runs[:m]
+        runs[-1] -= int(cum[m - 1] - n)
+        vals = torch.from_numpy(rng.integers(0, 65536, size=m, dtype=np.int64)).to(dev)
+        return torch.repeat_interleave(vals, torch.from_numpy(runs).to(dev)).to(torch.int32)
+    raise ValueError(kind)
+
+
+def bench_skewed(args, lib, wah, torch, dev, stream):
+    """C3: skewed and clustered single columns of args.n rows, bound 65535."""
+    out = {}
+    for kind in ("zipf1.1", "distinct16", "runs1000"):
+        v = gen_skewed(kind, args.n, args.seed, torch, dev)
+        bufs = wah._Buffers(args.n, 65535, dev)
+        sh = stream.cuda_stream
+
+        def step():
+            rc = lib.wah_build(v.data_ptr(), args.n, 65535, bufs.keys.data_ptr(),
+                               bufs.offsets.data_ptr(), bufs.index.data_ptr(),
+                               bufs.counts.data_ptr(), bufs.ws.data_ptr(), bufs.ws_bytes, sh)
+            assert rc == 0
+        step()
+        ms = time_events(step, max(3, args.steps // 5), torch, stream)
+        c = bufs.counts.cpu().numpy().view(np.uint32)
+        assert c[3] == 0
+        out[kind] = {"rows_per_s": args.n / (ms / 1e3), "ms": ms, "keycnt": int(c[0]),
+                     "index_len": int(c[1]), "merged": int(c[2])}
+        del v, bufs
+        torch.cuda.empty_cache()
+    return out
+
+
+def bench_batched(args, lib, wah, torch, dev, stream):
+    """C4: 4,096 columns, rows log-uniform in [1,024, 4,194,304], cardinality
+    log-uniform in [2, 65,536], values uniform within it.  Batched (one
+    launch sequence, replayed CUDA graph) against the plain path (one
+    wah_build per column on the same stream)."""
+    rng = np.random.default_rng(args.seed + 4)
+    ncols = args.batch_cols
+    sizes = np.rint(np.exp(rng.uniform(np.log(1024), np.log(4194304), ncols))).astype(np.int64)
+    cards = np.rint(np.exp(rng.uniform(np.log(2), np.log(65536), ncols))).astype(np.int64)
+    g = torch.Generator(device=dev)
+    g.manual_seed(args.seed + 4)
+    cols = [torch.randint(0, int(c), (int(n),), generator=g, device=dev, dtype=torch.int32)
+            for n, c in zip(sizes, cards)]
+    bounds = [int(c) - 1 for c in cards]
+    b = wah.Batch(sizes.tolist(), bounds)
+    outs = b.set_columns(cols, stream=stream)
+    b.launch_graph(stream)
+    ms_batched = time_events(lambda: b.launch_graph(stream), 3, torch, stream)
+    counts_b = torch.stack([o[3] for o in outs]).cpu().numpy().view(np.uint32).copy()
+    assert (counts_b[:, 3] == 0).all()
+    # plain path into the same outputs, one workspace sized for the largest column
+    nmax = int(sizes.max())
+    wsb = wah.workspace_bytes(nmax, 0)
+    ws = torch.empty(wsb, dtype=torch.uint8, device=dev)
+    sh = stream.cuda_stream
+
+    def plain():
+        for c in range(ncols):
+            keys, offs, index, cnt = outs[c]
+            rc = lib.wah_build(cols[c].data_ptr(), int(sizes[c]), bounds[c], keys.data_ptr(),
+                               offs.data_ptr(), index.data_ptr(), cnt.data_ptr(),
+                               ws.data_ptr(), wsb, sh)
+            assert rc == 0
+    plain()
+    ms_plain = time_events(plain, 2, torch, stream)
+    counts_p = torch.stack([o[3] for o in outs]).cpu().numpy().view(np.uint32)
+    same = bool((counts_p == counts_b).all())
+    total = int(sizes.sum())
+    b.close()
+    del cols, outs, ws
+    torch.cuda.empty_cache()
+    return {"columns": ncols, "rows": total, "ranges": None,
+            "rows_per_s_batched": total / (ms_batched / 1e3), "ms_batched": ms_batched,
+            "rows_per_s_plain": total / (ms_plain / 1e3), "ms_plain": ms_plain,
+            "speedup": ms_plain / ms_batched, "same_counts_as_plain": same}
+
+
+def bench_serving(args, wah, torch, dev):
+    """C5: Poisson arrivals of index-build requests (one pinned host column
+    each), rows log-uniform in [10,000, 16,777,216], values uniform [0,65535],
+    Zipf s=1.1 over 65,536 or run-clustered (mean run 1,000), 1/3 each;
+    64 GB device budget, results kept on the device.  Offered load: 80% of
+    the batching server's capacity measured on a saturating prefix of the
+    trace.  The continuous-batching server and the plain per-request server
+    replay the same trace."""
+    rng = np.random.default_rng(args.seed + 5)
+    nreq = args.serve_requests
+    max_rows = 16_777_216
+    sizes = np.rint(np.exp(rng.uniform(np.log(10_000), np.log(max_rows), nreq))).astype(np.int64)
+    kinds = rng.integers(0, 3, nreq)
+    pools = []
+    for kind in ("uniform", "zipf1.1", "runs1000"):
+        v = gen_skewed(kind, max_rows, args.seed + 5, torch, dev) if kind != "uniform" else \
+            torch.randint(0, 65536, (max_rows,), device=dev, dtype=torch.int32)
+        h = torch.empty(max_rows, dtype=torch.int32, pin_memory=True)
+        h.copy_(v)
+        pools.append(h)
+    del v
+    torch.cuda.empty_cache()
+
+    def run(plain, arrivals, count):
+        srv = wah.Server(budget_bytes=args.serve_budget_gb << 30, max_batch=512, streams=3,
+                         plain=plain)
+        ids = [srv.submit(pools[int(kinds[i])][:int(sizes[i])], bound=65535,
+                          delay=float(arrivals[i])) for i in range(count)]
+        t0 = time.perf_counter()
+        lat = np.empty(count)
+        for i, rid in enumerate(ids):
+            r = srv.wait(rid)
+            lat[i] = r.latency_s
+            srv.release(rid)
+        wall = time.perf_counter() - t0
+        srv.close()
+        rows = int(sizes[:count].sum())
+        return {"requests": count, "rows": rows, "wall_s": wall,
+                "rows_per_s": rows / wall,
+                "p50_ms": float(np.percentile(lat, 50) * 1e3),
+                "p99_ms": float(np.percentile(lat, 99) * 1e3),
+                "mean_ms": float(lat.mean() * 1e3)}
+
+    # capacity: a saturating prefix, everything arriving at once
+    cal = min(nreq, max(200, nreq // 10))
+    cap = run(False, np.zeros(cal), cal)["rows_per_s"]
+    rate = 0.8 * cap / float(sizes.mean())  # requests per second
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, nreq))
+    batched = run(False, arrivals, nreq)
+    plain = run(True, arrivals, nreq)
+    return {"requests": nreq, "offered_rows_per_s": 0.8 * cap, "capacity_rows_per_s": cap,
+            "arrival_rate_per_s": rate, "budget_gb": args.serve_budget_gb,
+            "batched": batched, "plain": plain,
+            "rows_per_s_ratio": batched["rows_per_s"] / plain["rows_per_s"],
+            "results_on_device": True}
 
 
 def cpu_oracle_rate(values: np.ndarray, sample: int, threads: int, repeats: int):
@@ -336,6 +506,10 @@ def main():
                "pipeline_depth": args.pipe_depth}
         pipe.close()
 
+    skewed = None if args.no_skewed else bench_skewed(args, lib, wah, torch, dev, stream)
+    batched = None if args.no_batched else bench_batched(args, lib, wah, torch, dev, stream)
+    serving = None if args.no_serving else bench_serving(args, wah, torch, dev)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         sample = min(args.cpu_sample, n)
@@ -368,6 +542,9 @@ def main():
             "gpu_launches": launches,
             "clocks": cl,
             "e2e": e2e,
+            "skewed": skewed,
+            "batched": batched,
+            "serving": serving,
             "cpu_baseline": cpu,
         }
         print(json.dumps(line), flush=True)

@@ -187,6 +187,43 @@ uint32_t wah_batch_ranges(const wah_batch* batch);
 void wah_batch_destroy(wah_batch* batch);
 
 /*
+ * Continuous-batching index server.  Requests (a host column each, with an
+ * arrival delay from now) are admitted in arrival order while their device
+ * memory fits `budget_bytes` (one device arena, allocated at create), batched
+ * into the batched build (up to max_batch columns per batch, `streams`
+ * batches in flight), and completed asynchronously; the outputs stay
+ * resident on the device until released.  The reference's `gpu` program
+ * keeps --jobs batches in flight between its indexer and merger actors
+ * (src/gpu.cpp:103-261).  plain != 0 builds every request alone with
+ * wah_build, one at a time (the per-request baseline).  h_values must stay
+ * valid until the request completes.  A request that cannot fit the budget
+ * even alone is refused with WAH_ENOMEM.  wah_server_wait blocks until the
+ * request is done and fills `result` (device pointers valid until
+ * wah_server_release; latency = completion - arrival).
+ */
+typedef struct wah_server wah_server;
+typedef struct wah_server_result {
+  wah_counts counts;
+  uint32_t* keys; /* device */
+  uint32_t* offsets;
+  uint32_t* index;
+  double latency_s; /* completion - arrival */
+  double queue_s;   /* admission - arrival */
+} wah_server_result;
+int wah_server_create(uint64_t budget_bytes, uint32_t max_batch, uint32_t streams,
+                      int plain, wah_server** out);
+int wah_server_submit(wah_server* server, const uint32_t* h_values, uint64_t n,
+                      uint32_t bound, double arrival_delay_s, uint64_t* id);
+int wah_server_wait(wah_server* server, uint64_t id, wah_server_result* result);
+int wah_server_release(wah_server* server, uint64_t id);
+/* Copies a completed request's keys[K], offsets[K], index[L] into caller
+ * device buffers on `stream` (before releasing it). */
+int wah_server_copy_out(wah_server* server, uint64_t id, uint32_t* d_keys,
+                        uint32_t* d_offsets, uint32_t* d_index, void* stream);
+uint64_t wah_server_arena_used(wah_server* server);
+void wah_server_destroy(wah_server* server);
+
+/*
  * Pipelined host-buffer builds: the reference's per-column flow
  * (global_argument -> phases -> mem_ref::data, src/phases.cpp:720-1088) with
  * several columns in flight, like `gpu --jobs` (src/gpu.cpp:194-259).  A pipe

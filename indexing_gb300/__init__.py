@@ -29,7 +29,7 @@ from . import _lib
 from ._lib import wah_counts
 
 __all__ = ["WahError", "WahIndex", "build_index", "sort_rids_by_value", "build_sorted",
-           "HostContext", "Pipeline", "Batch", "decoded_bitmap", "workspace_bytes", "output_caps",
+           "HostContext", "Pipeline", "Batch", "Server", "decoded_bitmap", "workspace_bytes", "output_caps",
            "MAX_ROWS", "last_launch_count"]
 
 MAX_ROWS = 1 << 30
@@ -343,6 +343,77 @@ class Batch:
     def close(self):
         if self._h:
             self._lib.wah_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """Continuous-batching index server (``wah_server_*``).
+
+    ``submit(values, bound, delay)`` queues a pinned host column arriving
+    ``delay`` seconds from now and returns an id; ``wait(id)`` blocks until it
+    is built and returns its :class:`wah_server_result` (device pointers stay
+    valid until ``release(id)``); ``result(id)`` also copies the index out as
+    a :class:`WahIndex` of CUDA tensors and releases it.
+    """
+
+    def __init__(self, budget_bytes: int = 64 << 30, max_batch: int = 1024, streams: int = 3,
+                 plain: bool = False):
+        self._lib = _lib.load()
+        h = ctypes.c_void_p()
+        _check(self._lib.wah_server_create(budget_bytes, max_batch, streams, int(plain),
+                                           ctypes.byref(h)), "wah_server_create")
+        self._h = h
+        self._keep = {}
+
+    def submit(self, values, bound: int = 0, delay: float = 0.0) -> int:
+        if hasattr(values, "data_ptr"):
+            ptr, n = values.data_ptr(), values.numel()
+        else:
+            ptr, n = values.ctypes.data, values.size
+        i = ctypes.c_uint64()
+        _check(self._lib.wah_server_submit(self._h, ptr, n, bound, delay, ctypes.byref(i)),
+               "wah_server_submit")
+        self._keep[i.value] = values
+        return i.value
+
+    def wait(self, rid: int):
+        res = _lib.wah_server_result()
+        rc = self._lib.wah_server_wait(self._h, rid, ctypes.byref(res))
+        self._keep.pop(rid, None)
+        _check(rc, "wah_server_wait")
+        return res
+
+    def release(self, rid: int) -> None:
+        _check(self._lib.wah_server_release(self._h, rid), "wah_server_release")
+
+    def result(self, rid: int) -> WahIndex:
+        """Wait, copy the outputs into fresh CUDA tensors, release."""
+        torch = _torch()
+        res = self.wait(rid)
+        K, L = res.counts.keycnt, res.counts.index_len
+        keys = torch.empty(max(K, 1), dtype=torch.int32, device="cuda")
+        offs = torch.empty(max(K, 1), dtype=torch.int32, device="cuda")
+        index = torch.empty(max(L, 1), dtype=torch.int32, device="cuda")
+        _check(self._lib.wah_server_copy_out(self._h, rid, keys.data_ptr(), offs.data_ptr(),
+                                             index.data_ptr(), _stream_handle(None)),
+               "wah_server_copy_out")
+        torch.cuda.current_stream().synchronize()
+        self.release(rid)
+        return WahIndex(keys[:K], offs[:K], index[:L], res.counts.merged)
+
+    @property
+    def arena_used(self) -> int:
+        return int(self._lib.wah_server_arena_used(self._h))
+
+    def close(self):
+        if self._h:
+            self._lib.wah_server_destroy(self._h)
             self._h = None
 
     def __del__(self):

@@ -20,7 +20,7 @@ OBJ_DIR = os.path.join(PKG_DIR, "_build")
 LIB_PATH = os.path.join(PKG_DIR, "libwah_gb300.so")
 
 CUDA_SOURCES = ["wah_sort.cu", "wah_index.cu", "wah_api.cu", "wah_batch.cu", "wah_pipe.cu",
-                "wah_noalloc.cu"]
+                "wah_serve.cu", "wah_noalloc.cu"]
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo",
               "-std=c++17", "-Xcompiler", "-fPIC", "-I" + INCLUDE, "-I" + CSRC]
 
@@ -65,6 +65,12 @@ class wah_counts(ctypes.Structure):
                 ("merged", ctypes.c_uint32), ("status", ctypes.c_uint32)]
 
 
+class wah_server_result(ctypes.Structure):
+    _fields_ = [("counts", wah_counts), ("keys", ctypes.c_void_p), ("offsets", ctypes.c_void_p),
+                ("index", ctypes.c_void_p), ("latency_s", ctypes.c_double),
+                ("queue_s", ctypes.c_double)]
+
+
 class wah_column(ctypes.Structure):
     _fields_ = [("values", ctypes.c_void_p), ("n", ctypes.c_uint64), ("bound", ctypes.c_uint32),
                 ("reserved", ctypes.c_uint32), ("keys", ctypes.c_void_p),
@@ -99,6 +105,14 @@ SIGNATURES = {
     "wah_batch_device_bytes": ([_vp], ctypes.c_size_t),
     "wah_batch_ranges": ([_vp], _u32),
     "wah_batch_destroy": ([_vp], None),
+    "wah_server_create": ([_u64, _u32, _u32, ctypes.c_int, ctypes.POINTER(_vp)], ctypes.c_int),
+    "wah_server_submit": ([_vp, _vp, _u64, _u32, ctypes.c_double, ctypes.POINTER(_u64)],
+                          ctypes.c_int),
+    "wah_server_wait": ([_vp, _u64, ctypes.POINTER(wah_server_result)], ctypes.c_int),
+    "wah_server_release": ([_vp, _u64], ctypes.c_int),
+    "wah_server_arena_used": ([_vp], _u64),
+    "wah_server_copy_out": ([_vp, _u64, _vp, _vp, _vp, _vp], ctypes.c_int),
+    "wah_server_destroy": ([_vp], None),
     "wah_pipe_create": ([_u64, _u32, _u32, ctypes.POINTER(_vp)], ctypes.c_int),
     "wah_pipe_submit": ([_vp, _vp, _u64, _vp, _vp, _vp, _vp, ctypes.POINTER(_u64)],
                         ctypes.c_int),

@@ -44,34 +44,141 @@ __global__ void k_batch_reset(const ColumnView* __restrict__ cols, uint32_t ncol
 
 }  // namespace
 
+namespace wah {
+
+void plan_batch_layout(const uint64_t* ns, const uint32_t* bounds, uint32_t ncols, int sms,
+                       BatchLayout* L) {
+  L->ncols = ncols;
+  L->max_passes = 1;
+  for (uint32_t c = 0; c < ncols; ++c)
+    L->max_passes = std::max(L->max_passes, passes_for_bound(bounds ? bounds[c] : 0));
+  // Range size: about 8 ranges per resident scatter CTA over the whole batch,
+  // whole radix tiles, and at most kMaxRanges ranges per column.
+  uint64_t total = 0, nmax = 0;
+  for (uint32_t c = 0; c < ncols; ++c) {
+    total += ns[c];
+    nmax = std::max<uint64_t>(nmax, ns[c]);
+  }
+  uint64_t rr = ceil_div(std::max<uint64_t>(total, 1), (uint64_t)std::max(sms, 1) * 2 * 8);
+  rr = std::max<uint64_t>(rr, ceil_div(nmax, kMaxRanges));
+  rr = std::max<uint64_t>(ceil_div(rr, kRangeQuantum) * kRangeQuantum, kRangeQuantum);
+  // Largest columns first: their long ranges start early, small ones fill
+  // the tail.  A column's ranges are contiguous.
+  std::vector<uint32_t> order(ncols);
+  std::iota(order.begin(), order.end(), 0u);
+  std::stable_sort(order.begin(), order.end(),
+                   [&](uint32_t x, uint32_t y) { return ns[x] > ns[y]; });
+  L->ranges.clear();
+  L->spans.assign(2 * (ncols + 1), 0);
+  for (uint32_t oc : order) {
+    L->spans[oc] = (uint32_t)L->ranges.size();
+    for (uint64_t lo = 0; lo < ns[oc]; lo += rr) {
+      RangeView v;
+      v.col = oc;
+      v.pad = 0;
+      v.lo = lo;
+      v.hi = std::min(lo + rr, ns[oc]);
+      L->ranges.push_back(v);
+    }
+    L->spans[ncols + 1 + oc] = (uint32_t)L->ranges.size();
+  }
+  L->nranges = (uint32_t)L->ranges.size();
+  L->buf_off.resize(ncols);
+  uint64_t rows = 0;
+  for (uint32_t c = 0; c < ncols; ++c) {
+    L->buf_off[c] = rows;
+    rows += ceil_div(std::max<uint64_t>(ns[c], 1), 64) * 64;  // 256-byte aligned columns
+  }
+  const uint32_t R = std::max<uint32_t>(L->nranges, 1);
+  size_t off = 0;
+  L->o_cols = off;
+  off += align_up(sizeof(ColumnView) * ncols);
+  L->o_ranges = off;
+  off += align_up(sizeof(RangeView) * R);
+  L->o_spans = off;
+  off += align_up(sizeof(uint32_t) * 2 * (ncols + 1));
+  L->o_ctrl = off;
+  off += align_up(sizeof(WahCtrl) * ncols);
+  L->o_hist = off;
+  off += align_up((size_t)kDigits * R * kRadix * 4);
+  L->o_start = off;
+  off += align_up((size_t)R * kRadix * 4);
+  L->o_counts = off;
+  off += align_up((size_t)R * 4 * 4);
+  L->o_rfirst = off;
+  off += align_up((size_t)R * 2 * 4);
+  L->col_bytes = align_up(rows * 4);
+  L->o_buf = off;
+  off += 4 * L->col_bytes;
+  L->bytes = off;
+}
+
+void fill_batch_columns(const BatchLayout& L, unsigned char* dev, const wah_column* cols,
+                        ColumnView* out) {
+  uint32_t* ka = reinterpret_cast<uint32_t*>(dev + L.o_buf);
+  uint32_t* ra = reinterpret_cast<uint32_t*>(dev + L.o_buf + L.col_bytes);
+  uint32_t* kb = reinterpret_cast<uint32_t*>(dev + L.o_buf + 2 * L.col_bytes);
+  uint32_t* rb = reinterpret_cast<uint32_t*>(dev + L.o_buf + 3 * L.col_bytes);
+  WahCtrl* ctrl = reinterpret_cast<WahCtrl*>(dev + L.o_ctrl);
+  for (uint32_t c = 0; c < L.ncols; ++c) {
+    const wah_column& x = cols[c];
+    ColumnView& v = out[c];
+    std::memset(&v, 0, sizeof(v));
+    v.input = x.values;
+    v.input_rids = nullptr;
+    v.keys_a = ka + L.buf_off[c];
+    v.rids_a = ra + L.buf_off[c];
+    v.keys_b = kb + L.buf_off[c];
+    v.rids_b = rb + L.buf_off[c];
+    v.n = x.n;
+    v.ctrl = ctrl + c;
+    v.keys = x.keys;
+    v.offsets = x.offsets;
+    v.index = x.index;
+    wah_output_caps(x.n, x.bound, &v.keys_cap, &v.index_cap);
+    v.counts = x.counts;
+    v.status = &x.counts->status;
+    v.passes = passes_for_bound(x.bound);
+    v.fixed_sel = -1;
+  }
+}
+
+cudaError_t enqueue_batch(const BatchLayout& L, unsigned char* dev, cudaStream_t s,
+                          uint32_t* launches) {
+  const LaunchOpts o = launch_opts(L.max_passes, nullptr);
+  if (o.sm_count <= 0) return cudaErrorNoDevice;
+  ColumnView* d_cols = reinterpret_cast<ColumnView*>(dev + L.o_cols);
+  cudaError_t e = cudaMemsetAsync(dev + L.o_ctrl, 0, sizeof(WahCtrl) * L.ncols, s);
+  if (e != cudaSuccess) return e;
+  k_batch_reset<<<(unsigned)ceil_div(L.ncols, 256), 256, 0, s>>>(d_cols, L.ncols);
+  ++*launches;
+  if (L.nranges == 0) return cudaGetLastError();
+  ManyColumns g;
+  g.cols = d_cols;
+  g.rngs = reinterpret_cast<const RangeView*>(dev + L.o_ranges);
+  g.col_first = reinterpret_cast<const uint32_t*>(dev + L.o_spans);
+  g.col_end = g.col_first + L.ncols + 1;
+  RangeArrays ra;
+  ra.hist = reinterpret_cast<uint32_t*>(dev + L.o_hist);
+  ra.start = reinterpret_cast<uint32_t*>(dev + L.o_start);
+  ra.counts = reinterpret_cast<uint32_t*>(dev + L.o_counts);
+  ra.first = reinterpret_cast<uint32_t*>(dev + L.o_rfirst);
+  ra.max_ranges = std::max<uint32_t>(L.nranges, 1);
+  e = launch_sort_many(g, L.ncols, L.nranges, ra, o, s, launches);
+  if (e != cudaSuccess) return e;
+  return launch_build_many(g, L.ncols, L.nranges, ra, o, s, launches);
+}
+
+}  // namespace wah
+
 struct wah_batch {
-  uint32_t ncols = 0;
-  uint32_t ranges = 0;
-  int max_passes = 1;
+  BatchLayout L;
   std::vector<uint64_t> n;
   std::vector<uint32_t> bound;
-  std::vector<uint32_t> order;       // columns by decreasing n (range order)
-  std::vector<uint64_t> buf_off;     // row offset of each column in the ping-pong arrays
-  std::vector<uint32_t> col_first;   // by column id: first range (+ end in [ncols])
-  std::vector<RangeView> host_ranges;
-  // device memory (one allocation)
   unsigned char* dev = nullptr;
-  size_t dev_bytes = 0;
-  ColumnView* d_cols = nullptr;
-  RangeView* d_ranges = nullptr;
-  uint32_t* d_col_first = nullptr;
-  WahCtrl* d_ctrl = nullptr;
-  uint32_t* d_keys_a = nullptr;
-  uint32_t* d_rids_a = nullptr;
-  uint32_t* d_keys_b = nullptr;
-  uint32_t* d_rids_b = nullptr;
-  RangeArrays ra{};
-  // pinned staging of the column table (source of its async upload)
-  ColumnView* h_cols = nullptr;
+  ColumnView* h_cols = nullptr;  // pinned staging of the column table
   bool columns_set = false;
-  // captured graph of wah_batch_build
   cudaGraphExec_t graph = nullptr;
-  cudaStream_t graph_stream = nullptr;
 };
 
 extern "C" {
@@ -84,9 +191,9 @@ void wah_batch_destroy(wah_batch* b) {
   delete b;
 }
 
-size_t wah_batch_device_bytes(const wah_batch* b) { return b ? b->dev_bytes : 0; }
+size_t wah_batch_device_bytes(const wah_batch* b) { return b ? b->L.bytes : 0; }
 
-uint32_t wah_batch_ranges(const wah_batch* b) { return b ? b->ranges : 0; }
+uint32_t wah_batch_ranges(const wah_batch* b) { return b ? b->L.nranges : 0; }
 
 int wah_batch_create(const uint64_t* ns, const uint32_t* bounds, uint32_t ncols,
                      wah_batch** out) {
@@ -96,103 +203,18 @@ int wah_batch_create(const uint64_t* ns, const uint32_t* bounds, uint32_t ncols,
     if (ns[c] >= WAH_MAX_ROWS) return WAH_ERANGE;
   wah_batch* b = new (std::nothrow) wah_batch;
   if (!b) return WAH_ENOMEM;
-  b->ncols = ncols;
   b->n.assign(ns, ns + ncols);
   b->bound.assign(ncols, 0);
   if (bounds) b->bound.assign(bounds, bounds + ncols);
-  for (uint32_t c = 0; c < ncols; ++c)
-    b->max_passes = std::max(b->max_passes, passes_for_bound(b->bound[c]));
-
-  // Range size: about 8 ranges per resident scatter CTA over the whole batch,
-  // whole radix tiles, and at most kMaxRanges ranges per column.
-  const int sms = std::max(sm_count_current(), 1);
-  const uint64_t total = std::accumulate(b->n.begin(), b->n.end(), (uint64_t)0);
-  const uint64_t nmax = *std::max_element(b->n.begin(), b->n.end());
-  uint64_t rr = ceil_div(std::max<uint64_t>(total, 1), (uint64_t)sms * 2 * 8);
-  rr = std::max<uint64_t>(rr, ceil_div(nmax, kMaxRanges));
-  rr = std::max<uint64_t>(ceil_div(rr, kRangeQuantum) * kRangeQuantum, kRangeQuantum);
-
-  // Largest columns first: their long ranges start early, small ones fill
-  // the tail.  A column's ranges are contiguous.
-  b->order.resize(ncols);
-  std::iota(b->order.begin(), b->order.end(), 0u);
-  std::stable_sort(b->order.begin(), b->order.end(),
-                   [&](uint32_t x, uint32_t y) { return b->n[x] > b->n[y]; });
-  b->col_first.assign(ncols + 1, 0);
-  std::vector<uint32_t> col_end(ncols, 0);
-  for (uint32_t oc : b->order) {
-    b->col_first[oc] = (uint32_t)b->host_ranges.size();
-    for (uint64_t lo = 0; lo < b->n[oc]; lo += rr) {
-      RangeView v;
-      v.col = oc;
-      v.pad = 0;
-      v.lo = lo;
-      v.hi = std::min(lo + rr, b->n[oc]);
-      b->host_ranges.push_back(v);
-    }
-    col_end[oc] = (uint32_t)b->host_ranges.size();
-  }
-  b->ranges = (uint32_t)b->host_ranges.size();
-  b->buf_off.resize(ncols);
-  uint64_t rows = 0;
-  for (uint32_t c = 0; c < ncols; ++c) {
-    b->buf_off[c] = rows;
-    rows += ceil_div(std::max<uint64_t>(b->n[c], 1), 64) * 64;  // 256-byte aligned columns
-  }
-
-  // Device layout.
-  const uint32_t R = std::max<uint32_t>(b->ranges, 1);
-  size_t off = 0;
-  const size_t o_cols = off;
-  off += align_up(sizeof(ColumnView) * ncols);
-  const size_t o_ranges = off;
-  off += align_up(sizeof(RangeView) * R);
-  const size_t o_first = off;
-  off += align_up(sizeof(uint32_t) * 2 * (ncols + 1));
-  const size_t o_ctrl = off;
-  off += align_up(sizeof(WahCtrl) * ncols);
-  const size_t o_hist = off;
-  off += align_up((size_t)kDigits * R * kRadix * 4);
-  const size_t o_start = off;
-  off += align_up((size_t)R * kRadix * 4);
-  const size_t o_counts = off;
-  off += align_up((size_t)R * 4 * 4);
-  const size_t o_rfirst = off;
-  off += align_up((size_t)R * 2 * 4);
-  const size_t col_bytes = align_up(rows * 4);
-  const size_t o_buf = off;
-  off += 4 * col_bytes;
-  b->dev_bytes = off;
-  cudaError_t e = cudaMalloc(&b->dev, off);
+  plan_batch_layout(ns, b->bound.data(), ncols, sm_count_current(), &b->L);
+  cudaError_t e = cudaMalloc(&b->dev, b->L.bytes);
   if (e == cudaSuccess) e = cudaMallocHost(&b->h_cols, sizeof(ColumnView) * ncols);
-  if (e != cudaSuccess) {
-    wah_batch_destroy(b);
-    return cuda_status(e);
-  }
-  b->d_cols = reinterpret_cast<ColumnView*>(b->dev + o_cols);
-  b->d_ranges = reinterpret_cast<RangeView*>(b->dev + o_ranges);
-  b->d_col_first = reinterpret_cast<uint32_t*>(b->dev + o_first);
-  b->d_ctrl = reinterpret_cast<WahCtrl*>(b->dev + o_ctrl);
-  b->ra.hist = reinterpret_cast<uint32_t*>(b->dev + o_hist);
-  b->ra.start = reinterpret_cast<uint32_t*>(b->dev + o_start);
-  b->ra.counts = reinterpret_cast<uint32_t*>(b->dev + o_counts);
-  b->ra.first = reinterpret_cast<uint32_t*>(b->dev + o_rfirst);
-  b->ra.max_ranges = R;
-  b->d_keys_a = reinterpret_cast<uint32_t*>(b->dev + o_buf);
-  b->d_rids_a = reinterpret_cast<uint32_t*>(b->dev + o_buf + col_bytes);
-  b->d_keys_b = reinterpret_cast<uint32_t*>(b->dev + o_buf + 2 * col_bytes);
-  b->d_rids_b = reinterpret_cast<uint32_t*>(b->dev + o_buf + 3 * col_bytes);
-
-  // Static tables: ranges and per-column range spans ([c] first, [ncols+1+c] end).
-  std::vector<uint32_t> spans(2 * (ncols + 1), 0);
-  for (uint32_t c = 0; c < ncols; ++c) {
-    spans[c] = b->col_first[c];
-    spans[ncols + 1 + c] = col_end[c];
-  }
-  e = cudaMemcpy(b->d_ranges, b->host_ranges.data(), sizeof(RangeView) * b->ranges,
-                 cudaMemcpyHostToDevice);
   if (e == cudaSuccess)
-    e = cudaMemcpy(b->d_col_first, spans.data(), spans.size() * 4, cudaMemcpyHostToDevice);
+    e = cudaMemcpy(b->dev + b->L.o_ranges, b->L.ranges.data(),
+                   sizeof(RangeView) * b->L.nranges, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(b->dev + b->L.o_spans, b->L.spans.data(), b->L.spans.size() * 4,
+                   cudaMemcpyHostToDevice);
   if (e != cudaSuccess) {
     wah_batch_destroy(b);
     return cuda_status(e);
@@ -203,7 +225,7 @@ int wah_batch_create(const uint64_t* ns, const uint32_t* bounds, uint32_t ncols,
 
 int wah_batch_set_columns(wah_batch* b, const wah_column* cols, void* stream) {
   if (!b || !cols) return WAH_EINVAL;
-  for (uint32_t c = 0; c < b->ncols; ++c) {
+  for (uint32_t c = 0; c < b->L.ncols; ++c) {
     const wah_column& x = cols[c];
     if (x.n != b->n[c] || x.bound != b->bound[c]) return WAH_EINVAL;
     if (!x.counts || (reinterpret_cast<uintptr_t>(x.counts) & 15)) return WAH_EINVAL;
@@ -214,28 +236,8 @@ int wah_batch_set_columns(wah_batch* b, const wah_column* cols, void* stream) {
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   cudaError_t e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return cuda_status(e);
-  for (uint32_t c = 0; c < b->ncols; ++c) {
-    const wah_column& x = cols[c];
-    ColumnView& v = b->h_cols[c];
-    std::memset(&v, 0, sizeof(v));
-    v.input = x.values;
-    v.input_rids = nullptr;
-    v.keys_a = b->d_keys_a + b->buf_off[c];
-    v.rids_a = b->d_rids_a + b->buf_off[c];
-    v.keys_b = b->d_keys_b + b->buf_off[c];
-    v.rids_b = b->d_rids_b + b->buf_off[c];
-    v.n = x.n;
-    v.ctrl = b->d_ctrl + c;
-    v.keys = x.keys;
-    v.offsets = x.offsets;
-    v.index = x.index;
-    wah_output_caps(x.n, x.bound, &v.keys_cap, &v.index_cap);
-    v.counts = x.counts;
-    v.status = &x.counts->status;
-    v.passes = passes_for_bound(x.bound);
-    v.fixed_sel = -1;
-  }
-  e = cudaMemcpyAsync(b->d_cols, b->h_cols, sizeof(ColumnView) * b->ncols,
+  fill_batch_columns(b->L, b->dev, cols, b->h_cols);
+  e = cudaMemcpyAsync(b->dev + b->L.o_cols, b->h_cols, sizeof(ColumnView) * b->L.ncols,
                       cudaMemcpyHostToDevice, s);
   if (e != cudaSuccess) return cuda_status(e);
   b->columns_set = true;
@@ -243,26 +245,10 @@ int wah_batch_set_columns(wah_batch* b, const wah_column* cols, void* stream) {
 }
 
 int wah_batch_build(wah_batch* b, void* stream) {
-  if (!b) return WAH_EINVAL;
-  if (!b->columns_set) return WAH_EINVAL;
+  if (!b || !b->columns_set) return WAH_EINVAL;
   uint32_t* launches = last_launches_slot();
   *launches = 0;
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
-  const LaunchOpts o = launch_opts(b->max_passes, nullptr);
-  if (o.sm_count <= 0) return WAH_ENODEV;
-  cudaError_t e = cudaMemsetAsync(b->d_ctrl, 0, sizeof(WahCtrl) * b->ncols, s);
-  if (e != cudaSuccess) return cuda_status(e);
-  k_batch_reset<<<ceil_div(b->ncols, 256), 256, 0, s>>>(b->d_cols, b->ncols);
-  ++*launches;
-  if (b->ranges == 0) return cuda_status(cudaGetLastError());
-  ManyColumns g;
-  g.cols = b->d_cols;
-  g.rngs = b->d_ranges;
-  g.col_first = b->d_col_first;
-  g.col_end = b->d_col_first + b->ncols + 1;
-  e = launch_sort_many(g, b->ncols, b->ranges, b->ra, o, s, launches);
-  if (e != cudaSuccess) return cuda_status(e);
-  return cuda_status(launch_build_many(g, b->ncols, b->ranges, b->ra, o, s, launches));
+  return cuda_status(enqueue_batch(b->L, b->dev, static_cast<cudaStream_t>(stream), launches));
 }
 
 int wah_batch_launch_graph(wah_batch* b, void* stream) {

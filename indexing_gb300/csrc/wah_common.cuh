@@ -9,6 +9,8 @@
 #pragma once
 
 #include <cstdint>
+#include <vector>
+
 #include <cuda_runtime.h>
 
 #include "wah/wah.h"
@@ -360,6 +362,28 @@ cudaError_t launch_build_many(const ManyColumns& g, uint32_t ncols, uint32_t ran
 constexpr uint64_t kRangeQuantum = 4096;
 cudaError_t launch_sort_deliver(const ColumnView& c, uint32_t* out_keys, uint32_t* out_rids,
                                 cudaStream_t s, uint32_t* launches);
+
+// Batched builds (wah_batch.cu): layout of one batch in one device block --
+// column table, ranges, per-column range spans, control blocks, range arrays
+// and the concatenated ping-pong buffers.
+struct BatchLayout {
+  uint32_t ncols = 0, nranges = 0;
+  int max_passes = 1;
+  std::vector<RangeView> ranges;
+  std::vector<uint32_t> spans;    // [c] first range, [ncols + 1 + c] end
+  std::vector<uint64_t> buf_off;  // row offset of each column in the buffers
+  size_t o_cols = 0, o_ranges = 0, o_spans = 0, o_ctrl = 0, o_hist = 0, o_start = 0,
+         o_counts = 0, o_rfirst = 0, o_buf = 0, col_bytes = 0, bytes = 0;
+};
+void plan_batch_layout(const uint64_t* ns, const uint32_t* bounds, uint32_t ncols, int sms,
+                       BatchLayout* L);
+// Column table for columns placed in `dev` (laid out by L); host memory.
+void fill_batch_columns(const BatchLayout& L, unsigned char* dev, const wah_column* cols,
+                        ColumnView* out);
+// Enqueue the whole build; the column, range and span tables must be in
+// `dev` already (stream-ordered before this).
+cudaError_t enqueue_batch(const BatchLayout& L, unsigned char* dev, cudaStream_t s,
+                          uint32_t* launches);
 
 // Shared host helpers (wah_api.cu).
 int passes_for_bound(uint32_t bound);
