@@ -249,6 +249,25 @@ int wah_pipe_submit(wah_pipe* pipe, const uint32_t* h_values, uint64_t n,
 int wah_pipe_wait(wah_pipe* pipe, uint64_t ticket);
 void wah_pipe_destroy(wah_pipe* pipe);
 
+/*
+ * Thin device helpers so host programs need only this header: device
+ * discovery and selection (the reference picks a device by name or the first
+ * available one, src/phases.cpp:376-388), device/pinned allocation, copies in
+ * either direction (cudaMemcpyDefault semantics; global_argument and
+ * mem_ref::data, src/phases.cpp:720, :1087-1088) and streams.
+ */
+int wah_device_count(void);
+int wah_device_name(int device, char* out, size_t cap);
+int wah_device_select(int device);
+int wah_dev_alloc(size_t bytes, void** out);
+void wah_dev_free(void* ptr);
+int wah_host_alloc(size_t bytes, void** out);
+void wah_host_free(void* ptr);
+int wah_copy(void* dst, const void* src, size_t bytes, void* stream);
+int wah_stream_create(void** out);
+int wah_stream_sync(void* stream);
+void wah_stream_destroy(void* stream);
+
 /* Number of kernels the last wah_build/wah_ctx_build_host on this thread
  * enqueued (launch accounting for benchmarks). */
 uint32_t wah_last_launch_count(void);

@@ -119,6 +119,17 @@ SIGNATURES = {
     "wah_pipe_wait": ([_vp, _u64], ctypes.c_int),
     "wah_pipe_destroy": ([_vp], None),
     "wah_last_launch_count": ([], _u32),
+    "wah_device_count": ([], ctypes.c_int),
+    "wah_device_name": ([ctypes.c_int, ctypes.c_char_p, ctypes.c_size_t], ctypes.c_int),
+    "wah_device_select": ([ctypes.c_int], ctypes.c_int),
+    "wah_dev_alloc": ([ctypes.c_size_t, ctypes.POINTER(_vp)], ctypes.c_int),
+    "wah_dev_free": ([_vp], None),
+    "wah_host_alloc": ([ctypes.c_size_t, ctypes.POINTER(_vp)], ctypes.c_int),
+    "wah_host_free": ([_vp], None),
+    "wah_copy": ([_vp, _vp, ctypes.c_size_t, _vp], ctypes.c_int),
+    "wah_stream_create": ([ctypes.POINTER(_vp)], ctypes.c_int),
+    "wah_stream_sync": ([_vp], ctypes.c_int),
+    "wah_stream_destroy": ([_vp], None),
     "wah_set_tuning": ([ctypes.c_int], ctypes.c_int),
     "wah_get_tuning": ([], ctypes.c_int),
     "wah_events_create": ([_u32, ctypes.POINTER(_vp)], ctypes.c_int),

@@ -384,3 +384,67 @@ int wah_ctx_build_host(wah_ctx* c, const uint32_t* h_values, uint64_t n, uint32_
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Thin device helpers for host programs that use only this header (the
+// reference's CAF OpenCL manager: find_device_if, global_argument,
+// mem_ref::data, dev->synchronize; src/phases.cpp:376-388, :720, :1087).
+// ---------------------------------------------------------------------------
+extern "C" {
+
+int wah_device_count(void) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) return 0;
+  return n;
+}
+
+int wah_device_name(int device, char* out, size_t cap) {
+  cudaDeviceProp p;
+  if (!out || cap == 0) return WAH_EINVAL;
+  cudaError_t e = cudaGetDeviceProperties(&p, device);
+  if (e != cudaSuccess) return cuda_status(e);
+  std::strncpy(out, p.name, cap - 1);
+  out[cap - 1] = '\0';
+  return WAH_OK;
+}
+
+int wah_device_select(int device) { return cuda_status(cudaSetDevice(device)); }
+
+int wah_dev_alloc(size_t bytes, void** out) {
+  if (!out) return WAH_EINVAL;
+  *out = nullptr;
+  return cuda_status(cudaMalloc(out, bytes ? bytes : 1));
+}
+
+void wah_dev_free(void* p) { cudaFree(p); }
+
+int wah_host_alloc(size_t bytes, void** out) {
+  if (!out) return WAH_EINVAL;
+  *out = nullptr;
+  return cuda_status(cudaMallocHost(out, bytes ? bytes : 1));
+}
+
+void wah_host_free(void* p) { cudaFreeHost(p); }
+
+int wah_copy(void* dst, const void* src, size_t bytes, void* stream) {
+  return cuda_status(
+      cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, static_cast<cudaStream_t>(stream)));
+}
+
+int wah_stream_create(void** out) {
+  if (!out) return WAH_EINVAL;
+  cudaStream_t s = nullptr;
+  cudaError_t e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+  *out = s;
+  return cuda_status(e);
+}
+
+int wah_stream_sync(void* stream) {
+  return cuda_status(cudaStreamSynchronize(static_cast<cudaStream_t>(stream)));
+}
+
+void wah_stream_destroy(void* stream) {
+  if (stream) cudaStreamDestroy(static_cast<cudaStream_t>(stream));
+}
+
+}  // extern "C"
