@@ -60,6 +60,57 @@ def build(verbose: bool = False) -> str:
     return LIB_PATH
 
 
+HOST_DIR = os.path.join(PKG_DIR, "host")
+BIN_DIR = os.path.join(PKG_DIR, "bin")
+# host programs: (source, links libwah_gb300.so)
+HOST_PROGRAMS = [("phases.cpp", True), ("gpu.cpp", True), ("generate.cpp", False),
+                 ("actors_test.cpp", False)]
+CXX_FLAGS = ["-O2", "-std=c++17", "-pthread", "-Wall", "-Wextra", "-I" + INCLUDE]
+
+
+def build_host(names=None) -> dict:
+    """Compile the C++ host programs into indexing_gb300/bin/ with g++.
+
+    phases and gpu link libwah_gb300.so (found next to the package through an
+    $ORIGIN rpath); generate and actors_test need no GPU library.  `names`
+    limits the build to some programs (e.g. ["actors_test", "generate"]).  Plain g++
+    without -march flags, so the same recipe builds on x86-64 and aarch64.
+    """
+    os.makedirs(BIN_DIR, exist_ok=True)
+    headers = [os.path.join(HOST_DIR, f) for f in os.listdir(HOST_DIR) if f.endswith(".hpp")]
+    headers.append(os.path.join(INCLUDE, "wah", "wah.h"))
+    newest_header = max(os.path.getmtime(h) for h in headers)
+    cxx = os.environ.get("CXX", "g++")
+
+    def compile_one(item):
+        src, link = item
+        out = os.path.join(BIN_DIR, src[:-4])
+        path = os.path.join(HOST_DIR, src)
+        deps = [os.path.getmtime(path), newest_header]
+        if link:
+            deps.append(os.path.getmtime(LIB_PATH))
+        if os.path.exists(out) and all(os.path.getmtime(out) >= t for t in deps):
+            return out
+        cmd = [cxx, *CXX_FLAGS, path, "-o", out]
+        if link:
+            cmd += ["-L" + PKG_DIR, "-l:libwah_gb300.so", "-Wl,-rpath,$ORIGIN/.."]
+        subprocess.run(cmd, check=True)
+        return out
+
+    todo = [p for p in HOST_PROGRAMS if names is None or p[0][:-4] in names]
+    with ThreadPoolExecutor(max_workers=len(todo)) as ex:
+        outs = list(ex.map(compile_one, todo))
+    return {src[:-4]: out for (src, _), out in zip(todo, outs)}
+
+
+def program(name: str) -> str:
+    """Path of a built host program (raises if it has not been built)."""
+    path = os.path.join(BIN_DIR, name)
+    if not os.path.exists(path):
+        raise FileNotFoundError(f"{path} is missing: run build_host()")
+    return path
+
+
 class wah_counts(ctypes.Structure):
     _fields_ = [("keycnt", ctypes.c_uint32), ("index_len", ctypes.c_uint32),
                 ("merged", ctypes.c_uint32), ("status", ctypes.c_uint32)]

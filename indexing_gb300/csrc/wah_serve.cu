@@ -155,6 +155,9 @@ struct wah_server {
   std::condition_variable done_cv;  // completions
   std::unordered_map<uint64_t, Req> reqs;
   std::deque<uint64_t> waiting;  // arrival order
+  // set by an admission pass that stopped because the arena had no room for
+  // the first arrived request (not because nothing had arrived yet)
+  bool mem_blocked = false;
   uint64_t next_id = 1;
   bool stop = false;
   std::thread worker;
@@ -221,10 +224,14 @@ struct wah_server {
         size_t in_b, out_b;
         sizes(r.n, r.bound, &in_b, &out_b, &r.keys_cap, &r.index_cap);
         const size_t in_off = arena.alloc(in_b);
-        if (in_off == SIZE_MAX) break;
+        if (in_off == SIZE_MAX) {
+          mem_blocked = ids.empty();
+          break;
+        }
         const size_t out_off = arena.alloc(out_b);
         if (out_off == SIZE_MAX) {
           arena.release(in_off, in_b);
+          mem_blocked = ids.empty();
           break;
         }
         r.in_off = in_off;
@@ -256,7 +263,10 @@ struct wah_server {
         ids.pop_back();
         ns.pop_back();
         bounds.pop_back();
-        if (ids.empty()) return false;
+        if (ids.empty()) {
+          mem_blocked = true;
+          return false;
+        }
       }
       for (uint64_t id : ids) {
         Req& r = reqs[id];
@@ -350,13 +360,20 @@ struct wah_server {
         if (plain_ws_off != SIZE_MAX) arena.release(plain_ws_off, plain_ws_bytes);
         plain_ws_off = arena.alloc(need_ws);
         plain_ws_bytes = plain_ws_off == SIZE_MAX ? 0 : need_ws;
-        if (plain_ws_off == SIZE_MAX) return false;
+        if (plain_ws_off == SIZE_MAX) {
+          mem_blocked = true;
+          return false;
+        }
       }
       const size_t in_off = arena.alloc(in_b);
-      if (in_off == SIZE_MAX) return false;
+      if (in_off == SIZE_MAX) {
+        mem_blocked = true;
+        return false;
+      }
       const size_t out_off = arena.alloc(out_b);
       if (out_off == SIZE_MAX) {
         arena.release(in_off, in_b);
+        mem_blocked = true;
         return false;
       }
       r.in_off = in_off;
@@ -404,13 +421,15 @@ struct wah_server {
     return true;
   }
 
-  // With nothing in flight, a request that arrived but cannot be placed
-  // (fragmented arena) would wait forever: fail it instead.
+  // With nothing in flight, a request that arrived but found no room in the
+  // arena (fragmentation) would wait forever: fail it instead.  Only a pass
+  // that stopped for lack of room counts; one that found nothing arrived yet
+  // (the front request may arrive just after it) does not.
   void fail_unplaceable() {
     std::lock_guard<std::mutex> lk(mu);
-    if (waiting.empty()) return;
+    if (!mem_blocked || waiting.empty()) return;
+    mem_blocked = false;
     Req& r = reqs[waiting.front()];
-    if (r.arrival > now_s()) return;
     waiting.pop_front();
     fail_locked(r, WAH_ENOMEM);
   }
@@ -419,6 +438,10 @@ struct wah_server {
     cudaSetDevice(device);
     while (true) {
       reap();
+      {
+        std::lock_guard<std::mutex> lk(mu);
+        mem_blocked = false;
+      }
       bool launched = false, any_busy = false;
       for (BatchSlot& b : slots) {
         if (b.busy) {

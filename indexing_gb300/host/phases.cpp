@@ -1,0 +1,260 @@
+// phases -- the reference's multi-phase GPU driver rebuilt on the GB300
+// kernels (src/phases.cpp:356-1136).
+//
+// A device actor owns the column's device buffers and one stream; the main
+// thread is a scoped actor that drives the phases one request/reply round
+// trip at a time and prints the host time each one took, as the reference's
+// SHOW_TIME_CONSUMPTION build does ("N us" per line, src/phases.cpp:714-1127):
+//
+//   Transfer to     values host -> device         (global_argument, :720)
+//   Sort            stable radix sort carrying row ids (:730-813)
+//   Index           chunk ids + literals, OR-merge, fills, fuse, column
+//                   lengths, offsets, keys -- one fused pass here (:817-1083)
+//   Transfer back   keys, offsets, index device -> host (mem_ref::data, :1087-1093)
+//   Total
+//
+// Flags as the reference (-f data file, -b bound, -d device name, -p print)
+// plus --describe (label each line, the reference's WITH_DESCRIPTION build)
+// and --output FILE (binary result: K, L, keys, offsets, index).  Unlike the
+// reference, -p prints the index as the cpu program does, and the keys are
+// produced (the reference's phases never materialises them).
+#include <algorithm>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "actors.hpp"
+#include "cli.hpp"
+
+using namespace wahact;
+
+namespace {
+
+struct transfer_to_atom {};
+struct sort_atom {};
+struct index_atom {};
+struct transfer_back_atom {};
+struct quit_atom {};
+
+struct device_state {
+  int device = 0;  // made current at the start of every handler: handlers
+                   // run on whichever worker thread the system picks
+  void* stream = nullptr;
+  uint64_t n = 0;
+  uint32_t bound = 0;
+  uint64_t keys_cap = 0, index_cap = 0;
+  size_t ws_bytes = 0;
+  uint32_t *values = nullptr, *sorted = nullptr, *rids = nullptr, *keys = nullptr,
+           *offsets = nullptr, *index = nullptr, *status = nullptr;
+  wah_counts* counts = nullptr;
+  void* ws = nullptr;
+  wah_counts host_counts{};
+
+  int allocate(uint64_t rows, uint32_t b) {
+    n = rows;
+    bound = b;
+    wah_output_caps(n, bound, &keys_cap, &index_cap);
+    ws_bytes = wah_workspace_bytes(n, bound);
+    int rc = wah_stream_create(&stream);
+    const uint64_t n1 = std::max<uint64_t>(n, 1);
+    void* p = nullptr;
+    auto alloc = [&](size_t bytes, void** out) {
+      if (rc == WAH_OK) rc = wah_dev_alloc(bytes, out);
+    };
+    alloc(n1 * 4, &p);
+    values = static_cast<uint32_t*>(p);
+    alloc(n1 * 4, &p);
+    sorted = static_cast<uint32_t*>(p);
+    alloc(n1 * 4, &p);
+    rids = static_cast<uint32_t*>(p);
+    alloc(std::max<uint64_t>(keys_cap, 1) * 4, &p);
+    keys = static_cast<uint32_t*>(p);
+    alloc(std::max<uint64_t>(keys_cap, 1) * 4, &p);
+    offsets = static_cast<uint32_t*>(p);
+    alloc(std::max<uint64_t>(index_cap, 1) * 4, &p);
+    index = static_cast<uint32_t*>(p);
+    alloc(16, &p);
+    status = static_cast<uint32_t*>(p);
+    alloc(sizeof(wah_counts), &p);
+    counts = static_cast<wah_counts*>(p);
+    alloc(ws_bytes, &ws);
+    return rc;
+  }
+  void release() {
+    if (stream) wah_stream_sync(stream);
+    for (void* p : {static_cast<void*>(values), static_cast<void*>(sorted),
+                    static_cast<void*>(rids), static_cast<void*>(keys),
+                    static_cast<void*>(offsets), static_cast<void*>(index),
+                    static_cast<void*>(status), static_cast<void*>(counts), ws})
+      if (p) wah_dev_free(p);
+    if (stream) wah_stream_destroy(stream);
+    stream = nullptr;
+  }
+};
+
+int sync_rc(int rc, void* stream) { return rc != WAH_OK ? rc : wah_stream_sync(stream); }
+
+// The device actor: one handler per phase, each replying when its work is
+// finished on the device (the reference's kernel actors reply when their
+// OpenCL event completes).
+behavior device_actor(actor_ctx<device_state>& self) {
+  auto& s = self.state;
+  return {
+      handler_from<transfer_to_atom, const std::vector<uint32_t>*, uint32_t>(
+          [&](const actor& from, transfer_to_atom, const std::vector<uint32_t>* values,
+              uint32_t bound) {
+            wah_device_select(s.device);
+            int rc = s.allocate(values->size(), bound);
+            if (rc == WAH_OK && !values->empty())
+              rc = wah_copy(s.values, values->data(), values->size() * 4, s.stream);
+            self.send(from, transfer_to_atom{}, sync_rc(rc, s.stream));
+          }),
+      handler_from<sort_atom>([&](const actor& from, sort_atom) {
+        wah_device_select(s.device);
+        uint32_t status = WAH_OK;
+        int rc = wah_sort_rids_by_value(s.values, s.n, s.bound, s.sorted, s.rids, s.status, s.ws,
+                                        s.ws_bytes, s.stream);
+        if (rc == WAH_OK) rc = wah_copy(&status, s.status, 4, s.stream);
+        rc = sync_rc(rc, s.stream);
+        if (rc == WAH_OK && s.n > 0) rc = static_cast<int>(status);
+        self.send(from, sort_atom{}, rc);
+      }),
+      handler_from<index_atom>([&](const actor& from, index_atom) {
+        wah_device_select(s.device);
+        int rc = wah_build_sorted(s.sorted, s.rids, s.n, s.keys, s.offsets, s.index, s.counts,
+                                  s.ws, s.ws_bytes, s.stream);
+        if (rc == WAH_OK) rc = wah_copy(&s.host_counts, s.counts, sizeof(wah_counts), s.stream);
+        rc = sync_rc(rc, s.stream);
+        if (rc == WAH_OK) rc = static_cast<int>(s.host_counts.status);
+        self.send(from, index_atom{}, rc, s.host_counts);
+      }),
+      handler_from<transfer_back_atom>([&](const actor& from, transfer_back_atom) {
+        wah_device_select(s.device);
+        const wah_counts c = s.host_counts;
+        std::vector<uint32_t> keys(c.keycnt), offsets(c.keycnt), index(c.index_len);
+        int rc = WAH_OK;
+        if (c.index_len) rc = wah_copy(index.data(), s.index, index.size() * 4, s.stream);
+        if (rc == WAH_OK && c.keycnt)
+          rc = wah_copy(offsets.data(), s.offsets, offsets.size() * 4, s.stream);
+        if (rc == WAH_OK && c.keycnt) rc = wah_copy(keys.data(), s.keys, keys.size() * 4, s.stream);
+        self.send(from, transfer_back_atom{}, sync_rc(rc, s.stream), std::move(keys),
+                  std::move(offsets), std::move(index));
+      }),
+      handler<quit_atom>([&](quit_atom) {
+        wah_device_select(s.device);
+        s.release();
+        self.quit();
+      }),
+  };
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+  std::string filename, device_name, output;
+  uint32_t bound = 0;
+  bool print_results = false, describe = false;
+  const std::vector<wahcli::flag> flags = {
+      {"data-file", 'f', "file with test data (one value per line)", wahcli::flag::STRING, &filename},
+      {"bound", 'b', "maximum value (0 will scan values)", wahcli::flag::U32, &bound},
+      {"device", 'd', "device for computation (first available if not found)",
+       wahcli::flag::STRING, &device_name},
+      {"print", 'p', "print resulting bitmap index", wahcli::flag::BOOL, &print_results},
+      {"describe", 0, "label each timing line", wahcli::flag::BOOL, &describe},
+      {"output", 'o', "write K, L, keys, offsets, index (u32) to this file", wahcli::flag::STRING,
+       &output},
+  };
+  const int pf = wahcli::parse_flags(argc, argv, flags);
+  if (pf != 0) return pf > 0 ? 0 : 2;
+  if (filename.empty()) {
+    std::printf("A filename with test data is required, see --help for details.\n");
+    return 2;
+  }
+  std::vector<uint32_t> values;
+  if (!wahcli::read_values(filename, &values)) {
+    std::fprintf(stderr, "cannot read '%s'\n", filename.c_str());
+    return 2;
+  }
+  if (bound == 0 && !values.empty()) bound = *std::max_element(values.begin(), values.end());
+  const int dev = wahcli::find_device(device_name, true);
+  if (dev < 0) {
+    std::fprintf(stderr, "No device found.\n");
+    return 3;
+  }
+  if (wah_device_select(dev) != WAH_OK) {
+    std::fprintf(stderr, "cannot select device %d\n", dev);
+    return 3;
+  }
+
+  auto line = [&](const char* label, uint64_t us) {
+    if (describe)
+      std::printf("%-16s%llu us\n", label, (unsigned long long)us);
+    else
+      std::printf("%llu us\n", (unsigned long long)us);
+  };
+  int rc = WAH_OK;
+  std::vector<uint32_t> keys, offsets, index;
+  wah_counts counts{};
+  {
+    actor_system system{2};
+    actor device = system.spawn<device_state>([dev](actor_ctx<device_state>& self) {
+      self.state.device = dev;
+      return device_actor(self);
+    });
+    scoped_actor self{system};
+    const auto start = std::chrono::steady_clock::now();
+    auto from = start;
+    auto expect_ok = [&](int r) {
+      if (r != WAH_OK && rc == WAH_OK) rc = r;
+      return rc == WAH_OK;
+    };
+
+    self.send(device, transfer_to_atom{}, static_cast<const std::vector<uint32_t>*>(&values),
+              bound);
+    self.receive(handler<transfer_to_atom, int>([&](transfer_to_atom, int r) { expect_ok(r); }));
+    line("Transfer to:", wahcli::micros_since(from));
+    from = std::chrono::steady_clock::now();
+
+    if (rc == WAH_OK) {
+      self.send(device, sort_atom{});
+      self.receive(handler<sort_atom, int>([&](sort_atom, int r) { expect_ok(r); }));
+      line("Sort:", wahcli::micros_since(from));
+      from = std::chrono::steady_clock::now();
+    }
+    if (rc == WAH_OK) {
+      self.send(device, index_atom{});
+      self.receive(handler<index_atom, int, wah_counts>([&](index_atom, int r, wah_counts c) {
+        expect_ok(r);
+        counts = c;
+      }));
+      line("Index:", wahcli::micros_since(from));
+      from = std::chrono::steady_clock::now();
+    }
+    if (rc == WAH_OK) {
+      self.send(device, transfer_back_atom{});
+      self.receive(handler<transfer_back_atom, int, std::vector<uint32_t>, std::vector<uint32_t>,
+                           std::vector<uint32_t>>(
+          [&](transfer_back_atom, int r, std::vector<uint32_t> k, std::vector<uint32_t> o,
+              std::vector<uint32_t> i) {
+            expect_ok(r);
+            keys = std::move(k);
+            offsets = std::move(o);
+            index = std::move(i);
+          }));
+      line("Transfer back:", wahcli::micros_since(from));
+    }
+    line("Total:", wahcli::micros_since(start));
+    self.send(device, quit_atom{});
+  }
+  if (rc != WAH_OK) {
+    std::fprintf(stderr, "[!!!] %s\n", wah_strerror(rc));
+    return 1;
+  }
+  std::printf("Index has %u elements with %u keys\n", counts.index_len, counts.keycnt);
+  if (print_results) wahcli::print_index(keys, offsets, index);
+  if (!output.empty() && !wahcli::write_result(output, keys, offsets, index)) {
+    std::fprintf(stderr, "cannot write '%s'\n", output.c_str());
+    return 1;
+  }
+  return 0;
+}
