@@ -43,6 +43,7 @@ extern "C" {
 #define WAH_ERANGE 5    /* n >= 2^30, or a value above the stated bound     */
 #define WAH_EOVERFLOW 6 /* an output would exceed the caller's capacity     */
 #define WAH_ENODEV 7    /* no usable sm_103 device                          */
+#define WAH_ECORRUPT 8  /* index words do not describe the stated rows      */
 
 /* Largest column one call accepts (rows).  Offsets and index positions are
  * u32 as in the reference; n < 2^30 keeps every counter in range. */
@@ -267,6 +268,61 @@ int wah_copy(void* dst, const void* src, size_t bytes, void* stream);
 int wah_stream_create(void** out);
 int wah_stream_sync(void* stream);
 void wah_stream_destroy(void* stream);
+
+/*
+ * Decoding a built index on the device: the reference's decoded_bitmap
+ * (src/cpu.cpp:47-74; src/gpu.cpp:65-94) reads one key's words into a
+ * '0'/'1' string on the host; wah_decode reads every key's words at once.
+ * Inputs: keys[K], offsets[K], index[L] of a column of n rows (device).
+ * Optional outputs (device, NULL to skip):
+ *   d_rows[n]        row ids, keys ascending, rows ascending within a key
+ *                    (the stable sort's rid order)
+ *   d_row_values[n]  the key of each of those rows (the sorted column)
+ *   d_column[n]      the column itself: d_column[row] = its value
+ *   d_key_rows[K]    position in d_rows of each key's first row
+ * d_status (device u32): WAH_OK, or WAH_ECORRUPT when a row falls outside
+ * [0, n) or the words hold a number of rows other than n.  Workspace:
+ * wah_decode_workspace_bytes().  Enqueues on `stream`, no synchronisation.
+ */
+size_t wah_decode_workspace_bytes(void);
+int wah_decode(const uint32_t* d_keys, const uint32_t* d_offsets,
+               const uint32_t* d_index, uint32_t keycnt, uint32_t index_len,
+               uint64_t n, uint32_t* d_rows, uint32_t* d_row_values,
+               uint32_t* d_column, uint32_t* d_key_rows, uint32_t* d_status,
+               void* d_workspace, size_t workspace_bytes, void* stream);
+
+/*
+ * Queries on a built index (no counterpart in the reference, which stops at
+ * decoding).  Term A = rows whose value is in [a_lo, a_hi]; with op
+ * WAH_QUERY_OR / _AND / _ANDNOT, term B = [b_lo, b_hi] combines with it
+ * (A|B, A&B, A&~B); WAH_QUERY_KEYS is A alone.  A single key is
+ * [v, v]; a value range is a range of keys.  Outputs (device, NULL to skip):
+ *   d_words[words]  the result as a WAH bitmap in the index's format
+ *                   (literal per non-empty chunk, fills for gaps, no
+ *                   trailing fill): for one key, exactly its own words;
+ *                   capacity 2 * ceil(n / 31) always suffices
+ *   d_rows[rows]    the result's row ids, ascending; capacity n suffices
+ * d_result (device, 16-byte aligned) receives words, rows and a status
+ * (WAH_EOVERFLOW when a capacity was too small: counts stay exact, the
+ * outputs are cut).  Workspace: wah_query_workspace_bytes(n).
+ */
+#define WAH_QUERY_KEYS 0
+#define WAH_QUERY_OR 1
+#define WAH_QUERY_AND 2
+#define WAH_QUERY_ANDNOT 3
+typedef struct wah_query_result {
+  uint32_t words;
+  uint32_t rows;
+  uint32_t status;
+  uint32_t reserved;
+} wah_query_result;
+size_t wah_query_workspace_bytes(uint64_t n);
+int wah_query(const uint32_t* d_keys, const uint32_t* d_offsets,
+              const uint32_t* d_index, uint32_t keycnt, uint32_t index_len,
+              uint64_t n, uint32_t a_lo, uint32_t a_hi, int op, uint32_t b_lo,
+              uint32_t b_hi, uint32_t* d_words, uint64_t words_cap,
+              uint32_t* d_rows, uint64_t rows_cap, wah_query_result* d_result,
+              void* d_workspace, size_t workspace_bytes, void* stream);
 
 /* Number of kernels the last wah_build/wah_ctx_build_host on this thread
  * enqueued (launch accounting for benchmarks). */

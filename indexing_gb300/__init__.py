@@ -13,6 +13,11 @@ Python face of the C ABI in ``include/wah/wah.h`` (library
                              mem_ref::data flow)
 * :func:`decoded_bitmap`     one key's words as a '0'/'1' string
                              (src/cpu.cpp:47-74)
+* :func:`decode`             every key's rows on the GPU (row ids, the
+                             sorted column, the column itself)
+* :func:`query`              rows of a key / value range, or of two ranges
+                             combined (OR, AND, AND NOT), as row ids and as
+                             a WAH bitmap
 
 Device memory comes from torch (plumbing only); every computation runs in
 the CUDA kernels of the native library.  There is no CPU fallback: without
@@ -30,12 +35,14 @@ from ._lib import wah_counts
 
 __all__ = ["WahError", "WahIndex", "build_index", "sort_rids_by_value", "build_sorted",
            "HostContext", "Pipeline", "Batch", "Server", "decoded_bitmap", "workspace_bytes", "output_caps",
-           "MAX_ROWS", "last_launch_count"]
+           "MAX_ROWS", "last_launch_count", "decode", "query", "QUERY_KEYS", "QUERY_OR",
+           "QUERY_AND", "QUERY_ANDNOT"]
 
 MAX_ROWS = 1 << 30
 
 WAH_OK, WAH_EINVAL, WAH_ENOMEM, WAH_ECUDA, WAH_ETIMEOUT, WAH_ERANGE, WAH_EOVERFLOW, \
-    WAH_ENODEV = range(8)
+    WAH_ENODEV, WAH_ECORRUPT = range(9)
+QUERY_KEYS, QUERY_OR, QUERY_AND, QUERY_ANDNOT = range(4)
 
 
 class WahError(RuntimeError):
@@ -161,6 +168,101 @@ def build_index(values, bound: int = 0, stream=None, device="cuda", sync: bool =
         raise WahError(int(c[3]), "wah_build (device)")
     K, L, k = int(c[0]), int(c[1]), int(c[2])
     return WahIndex(b.keys[:K], b.offsets[:K], b.index[:L], k)
+
+
+def _index_tensors(idx: WahIndex):
+    torch = _torch()
+    parts = []
+    for a in (idx.keys, idx.offsets, idx.index):
+        t = _as_device_u32(a, "cuda") if isinstance(a, np.ndarray) else a
+        parts.append(t.contiguous())
+    dev = parts[2].device if parts[2].numel() else parts[0].device
+    # empty tensors may have no storage: give the kernels a valid pointer
+    parts = [t if t.numel() else torch.zeros(4, dtype=torch.int32, device=dev) for t in parts]
+    return parts[0], parts[1], parts[2], dev
+
+
+def decode(idx: WahIndex, n: int, rows: bool = True, values: bool = False,
+           column: bool = False, key_rows: bool = False, stream=None) -> dict:
+    """Decodes every key of ``idx`` (an index of ``n`` rows) on the GPU.
+
+    Returns a dict of CUDA int32 tensors (uint32 bits) for the outputs asked
+    for: ``rows`` (row ids, keys ascending, rows ascending per key),
+    ``values`` (the key of each of those rows), ``column`` (the column:
+    ``column[row]`` = its value; rows no key covers keep 0xFFFFFFFF) and
+    ``key_rows`` (position of each key's first row).  Raises WahError with
+    WAH_ECORRUPT when the words do not describe exactly n rows."""
+    lib = _lib.load()
+    torch = _torch()
+    keys, offsets, index, dev = _index_tensors(idx)
+    K, L = len(idx.keys), len(idx.index)
+    out = {}
+
+    def alloc(name, size, fill=None):
+        t = torch.empty(max(size, 1), dtype=torch.int32, device=dev)
+        if fill is not None:
+            t.fill_(fill)
+        out[name] = t
+        return t.data_ptr()
+
+    p_rows = alloc("rows", n) if rows else None
+    p_vals = alloc("values", n) if values else None
+    p_col = alloc("column", n, -1) if column else None
+    p_kr = alloc("key_rows", K) if key_rows else None
+    status = torch.zeros(4, dtype=torch.int32, device=dev)
+    wsb = int(lib.wah_decode_workspace_bytes())
+    ws = torch.empty(wsb, dtype=torch.uint8, device=dev)
+    rc = lib.wah_decode(keys.data_ptr(), offsets.data_ptr(), index.data_ptr(), K, L, n, p_rows,
+                        p_vals, p_col, p_kr, status.data_ptr(), ws.data_ptr(), wsb,
+                        _stream_handle(stream))
+    _check(rc, "wah_decode")
+    st = int(status[0].item())
+    if st != WAH_OK:
+        raise WahError(st, "wah_decode (device)")
+    sizes = {"rows": n, "values": n, "column": n, "key_rows": K}
+    return {k: v[:sizes[k]] for k, v in out.items()}
+
+
+def _term(t):
+    if t is None:
+        return 0, 0
+    if isinstance(t, (tuple, list)):
+        return int(t[0]), int(t[1])
+    return int(t), int(t)
+
+
+def query(idx: WahIndex, n: int, a, op: int = QUERY_KEYS, b=None, words: bool = True,
+          rows: bool = True, stream=None):
+    """Rows of ``idx`` (an index of ``n`` rows) whose value lies in term A
+    (a value ``v`` or an inclusive range ``(lo, hi)``), combined with term B
+    by ``op`` (QUERY_OR / QUERY_AND / QUERY_ANDNOT; QUERY_KEYS = A alone).
+
+    Returns ``(words, rows)``: the result as a WAH bitmap in the index's own
+    format and as ascending row ids (CUDA int32 tensors, uint32 bits; None
+    for an output not asked for)."""
+    lib = _lib.load()
+    torch = _torch()
+    keys, offsets, index, dev = _index_tensors(idx)
+    K, L = len(idx.keys), len(idx.index)
+    a_lo, a_hi = _term(a)
+    b_lo, b_hi = _term(b)
+    nchunks = (n + 30) // 31
+    wcap = 2 * nchunks
+    w_out = torch.empty(max(wcap, 1), dtype=torch.int32, device=dev) if words else None
+    r_out = torch.empty(max(n, 1), dtype=torch.int32, device=dev) if rows else None
+    res = torch.zeros(4, dtype=torch.int32, device=dev)
+    wsb = int(lib.wah_query_workspace_bytes(n))
+    ws = torch.empty(wsb, dtype=torch.uint8, device=dev)
+    rc = lib.wah_query(keys.data_ptr(), offsets.data_ptr(), index.data_ptr(), K, L, n, a_lo, a_hi,
+                       op, b_lo, b_hi, w_out.data_ptr() if words else None, wcap,
+                       r_out.data_ptr() if rows else None, n, res.data_ptr(), ws.data_ptr(), wsb,
+                       _stream_handle(stream))
+    _check(rc, "wah_query")
+    r = res.cpu().numpy().view(np.uint32)
+    if r[2] != WAH_OK:
+        raise WahError(int(r[2]), "wah_query (device)")
+    nw, nr = int(r[0]), int(r[1])
+    return (w_out[:nw] if words else None), (r_out[:nr] if rows else None)
 
 
 def sort_rids_by_value(values, bound: int = 0, stream=None, device="cuda"):

@@ -20,7 +20,7 @@ OBJ_DIR = os.path.join(PKG_DIR, "_build")
 LIB_PATH = os.path.join(PKG_DIR, "libwah_gb300.so")
 
 CUDA_SOURCES = ["wah_sort.cu", "wah_index.cu", "wah_api.cu", "wah_batch.cu", "wah_pipe.cu",
-                "wah_serve.cu", "wah_noalloc.cu"]
+                "wah_serve.cu", "wah_noalloc.cu", "wah_query.cu"]
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo",
               "-std=c++17", "-Xcompiler", "-fPIC", "-I" + INCLUDE, "-I" + CSRC]
 
@@ -169,6 +169,12 @@ SIGNATURES = {
                         ctypes.c_int),
     "wah_pipe_wait": ([_vp, _u64], ctypes.c_int),
     "wah_pipe_destroy": ([_vp], None),
+    "wah_decode_workspace_bytes": ([], ctypes.c_size_t),
+    "wah_decode": ([_vp, _vp, _vp, _u32, _u32, _u64, _vp, _vp, _vp, _vp, _vp, _vp,
+                    ctypes.c_size_t, _vp], ctypes.c_int),
+    "wah_query_workspace_bytes": ([_u64], ctypes.c_size_t),
+    "wah_query": ([_vp, _vp, _vp, _u32, _u32, _u64, _u32, _u32, ctypes.c_int, _u32, _u32,
+                   _vp, _u64, _vp, _u64, _vp, _vp, ctypes.c_size_t, _vp], ctypes.c_int),
     "wah_last_launch_count": ([], _u32),
     "wah_device_count": ([], ctypes.c_int),
     "wah_device_name": ([ctypes.c_int, ctypes.c_char_p, ctypes.c_size_t], ctypes.c_int),

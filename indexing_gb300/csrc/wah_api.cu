@@ -127,6 +127,7 @@ const char* wah_strerror(int status) {
     case WAH_ERANGE: return "value or size out of range";
     case WAH_EOVERFLOW: return "output capacity exceeded";
     case WAH_ENODEV: return "no usable sm_103 device";
+    case WAH_ECORRUPT: return "index words do not describe the stated rows";
     default: return "unknown status";
   }
 }
