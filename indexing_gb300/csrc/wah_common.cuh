@@ -120,6 +120,12 @@ __device__ __forceinline__ uint32_t bfe(uint32_t x, uint32_t pos, uint32_t len) 
   return r;
 }
 
+static_assert(kRadixBits == 8, "digits are bytes");
+// Byte `byte` (0..3) of x: an 8-bit radix digit in one byte permute.
+__device__ __forceinline__ uint32_t digit8(uint32_t x, uint32_t byte) {
+  return __byte_perm(x, 0u, 0x4440u | byte);
+}
+
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return (uint32_t)__cvta_generic_to_shared(p);
 }

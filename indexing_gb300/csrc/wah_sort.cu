@@ -47,9 +47,8 @@ struct WarpHist {
     const uint32_t varying = o ^ a;
 #pragma unroll
     for (int p = 0; p < DIGITS; ++p) {
-      const uint32_t pos = (first + p) * kRadixBits;
-      const uint32_t d = bfe(x, pos, kRadixBits);
-      if (bfe(varying, pos, kRadixBits) == 0) {
+      const uint32_t d = digit8(x, first + p);
+      if (digit8(varying, first + p) == 0) {
         if (lane == 0) atomicAdd(&h[p][d], 32u);
       } else {
         atomicAdd(&h[p][d], 1u);
@@ -60,7 +59,7 @@ struct WarpHist {
     acc_or |= x;
 #pragma unroll
     for (int p = 0; p < DIGITS; ++p)
-      atomicAdd(&h[p][bfe(x, (first + p) * kRadixBits, kRadixBits)], 1u);
+      atomicAdd(&h[p][digit8(x, first + p)], 1u);
   }
 };
 
@@ -319,7 +318,6 @@ __global__ void __launch_bounds__(kSortThreads, 2)
   uint32_t* status = col.status;
 
   const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const uint32_t shift = pass * kRadixBits;
   const uint64_t lo = rv.lo, hi = rv.hi;
   if (lo >= hi) return;
   const uint32_t ntiles = (uint32_t)ceil_div(hi - lo, TILE);
@@ -388,14 +386,14 @@ __global__ void __launch_bounds__(kSortThreads, 2)
 #pragma unroll
     for (int j = 0; j < ITEMS; ++j) {
       const bool ballot = PEERS == 0 || (PEERS == 2 && j >= HALF);
-      rank[j] = ballot ? digit_peers<true>(bfe(key[j], shift, kRadixBits))
-                       : digit_peers<false>(bfe(key[j], shift, kRadixBits));
+      rank[j] = ballot ? digit_peers<true>(digit8(key[j], pass))
+                       : digit_peers<false>(digit8(key[j], pass));
     }
 #pragma unroll
     for (int j = 0; j < HALF; ++j) {
       const uint32_t pa = rank[j], pb = rank[j + HALF];
-      const uint32_t da = bfe(key[j], shift, kRadixBits);
-      const uint32_t db = bfe(key[j + HALF], shift, kRadixBits);
+      const uint32_t da = digit8(key[j], pass);
+      const uint32_t db = digit8(key[j + HALF], pass);
       const uint32_t ca = whA[da];
       const uint32_t cb = whB[db];
       __syncwarp();
@@ -406,7 +404,7 @@ __global__ void __launch_bounds__(kSortThreads, 2)
       rank[j + HALF] = cb + __popc(pb & lt);
     }
 #pragma unroll
-    for (int j = HALF; j < ITEMS; ++j) rank[j] += whA[bfe(key[j], shift, kRadixBits)];
+    for (int j = HALF; j < ITEMS; ++j) rank[j] += whA[digit8(key[j], pass)];
     __syncthreads();
 
     // Thread b: tile count of bin b, tile-local bin start, warp starts.
@@ -438,7 +436,7 @@ __global__ void __launch_bounds__(kSortThreads, 2)
     const uint32_t rid0 = (uint32_t)base + row0;
 #pragma unroll
     for (int j = 0; j < ITEMS; ++j) {
-      const uint32_t r = whA[bfe(key[j], shift, kRadixBits)] + rank[j];
+      const uint32_t r = whA[digit8(key[j], pass)] + rank[j];
       out_keys[r] = key[j];
       sm.out_rids[r] = rin ? rsrc[j * 32] : rid0 + j * 32;
     }
@@ -451,7 +449,7 @@ __global__ void __launch_bounds__(kSortThreads, 2)
         const uint32_t k = it * kSortThreads + tid;
         if (k < valid) {
           const uint32_t kk = out_keys[k];
-          const uint32_t g = sm.bin_base[bfe(kk, shift, kRadixBits)] + k;
+          const uint32_t g = sm.bin_base[digit8(kk, pass)] + k;
           if (g < n32) {
             kout[g] = kk;
             rout[g] = sm.out_rids[k];
