@@ -19,6 +19,10 @@ SHOW_TIME_CONSUMPTION output, src/phases.cpp:714-1127) go to stderr.
               duration, against the measured HBM copy bandwidth
   cpu_baseline  the oracle (plain-C restatement of the reference `cpu`
               program) on a bounded sample, host cores of this machine
+  decode      the built index decoded back to row ids on the device, and
+              one-key / 1,000-key range queries
+  ingest      the column as a one-value-per-line text file parsed on the
+              device (resident text, and from pinned host memory)
 
 --impl reference times the reference CPU implementation (the oracle port:
 the reference's own sources are not on the GPU machine) on all host threads.
@@ -60,6 +64,8 @@ def parse():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--batch-cols", type=int, default=4096)
     ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--no-ingest", action="store_true")
+    ap.add_argument("--no-decode", action="store_true")
     ap.add_argument("--serve-requests", type=int, default=20000)
     ap.add_argument("--serve-budget-gb", type=int, default=64)
     ap.add_argument("--pipe-depth", type=int, default=3,
@@ -247,6 +253,116 @@ def bench_batched(args, lib, wah, torch, dev, stream):
             "rows_per_s_batched": total / (ms_batched / 1e3), "ms_batched": ms_batched,
             "rows_per_s_plain": total / (ms_plain / 1e3), "ms_plain": ms_plain,
             "speedup": ms_plain / ms_batched, "same_counts_as_plain": same}
+
+
+def column_text(col, max_digits, torch):
+    """The column as the reference's data file (`generate` format: one value
+    per line), built on the device: digits are scattered to each value's
+    offset in the text."""
+    v = col.to(torch.int64)
+    ndig = torch.ones_like(v)
+    t = v // 10
+    for _ in range(max_digits - 1):
+        ndig += (t > 0).to(torch.int64)
+        t //= 10
+    del t
+    ends = torch.cumsum(ndig + 1, 0)
+    starts = ends - ndig - 1
+    text = torch.full((int(ends[-1].item()),), 10, dtype=torch.uint8, device=col.device)
+    last = starts + ndig - 1
+    del ends, starts
+    x = v
+    for d in range(max_digits):
+        m = ndig > d
+        text[last[m] - d] = (x[m] % 10 + 48).to(torch.uint8)
+        x = x // 10
+    return text
+
+
+def bench_ingest(args, lib, torch, dev, stream, d_values, n):
+    """Text ingest: the column written as a one-value-per-line data file
+    (the reference's `generate` format), parsed by wah_parse_text from device
+    memory (value) and from pinned host memory with the copy in the timed
+    region (e2e).  The parsed column must equal the original."""
+    digits = len(str(args.card - 1))
+    text = column_text(d_values, digits, torch)
+    nbytes = text.numel()
+    out = torch.empty((nbytes + 1) // 2, dtype=torch.int32, device=dev)
+    res = torch.zeros(4, dtype=torch.int64, device=dev)
+    wsb = int(lib.wah_parse_workspace_bytes())
+    ws = torch.empty(wsb, dtype=torch.uint8, device=dev)
+    sh = stream.cuda_stream
+
+    def parse_dev(src=text):
+        rc = lib.wah_parse_text(src.data_ptr(), nbytes, out.data_ptr(), out.numel(),
+                                res.data_ptr(), ws.data_ptr(), wsb, sh)
+        assert rc == 0
+    parse_dev()
+    torch.cuda.synchronize()
+    count = int(res.cpu().numpy()[0])
+    same = count == n and bool(torch.equal(out[:n], d_values))
+    steps = max(3, args.steps // 5)
+    ms = time_events(parse_dev, steps, torch, stream)
+    host = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    host.copy_(text)
+    staging = torch.empty_like(text)
+
+    def parse_host():
+        staging.copy_(host, non_blocking=True)
+        parse_dev(staging)
+    parse_host()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        parse_host()
+    torch.cuda.synchronize()
+    dt = (time.perf_counter() - t0) / steps
+    del text, out, staging, host
+    torch.cuda.empty_cache()
+    return {"text_bytes": nbytes, "values": count, "parsed_equals_column": same,
+            "ms": ms, "rows_per_s": n / (ms / 1e3), "text_gb_per_s": nbytes / (ms / 1e3) / 1e9,
+            "alg_bytes": nbytes + 4 * n,
+            "e2e": {"rows_per_s": n / dt, "ms": dt * 1e3, "h2d_bytes_per_step": nbytes}}
+
+
+def bench_decode(args, lib, torch, dev, stream, bufs, n, K, L):
+    """Decode of the built index back to row ids on the device (wah_decode),
+    and one-key / value-range queries (wah_query)."""
+    rows = torch.empty(n, dtype=torch.int32, device=dev)
+    st = torch.zeros(4, dtype=torch.int32, device=dev)
+    wsb = int(lib.wah_decode_workspace_bytes())
+    ws = torch.empty(wsb, dtype=torch.uint8, device=dev)
+    sh = stream.cuda_stream
+
+    def dec():
+        rc = lib.wah_decode(bufs.keys.data_ptr(), bufs.offsets.data_ptr(), bufs.index.data_ptr(),
+                            K, L, n, rows.data_ptr(), None, None, None, st.data_ptr(),
+                            ws.data_ptr(), wsb, sh)
+        assert rc == 0
+    dec()
+    ms = time_events(dec, max(3, args.steps // 5), torch, stream)
+    assert int(st[0].item()) == 0
+    qws_b = int(lib.wah_query_workspace_bytes(n))
+    qws = torch.empty(qws_b, dtype=torch.uint8, device=dev)
+    qrows = torch.empty(n, dtype=torch.int32, device=dev)
+    qwords = torch.empty(2 * ((n + 30) // 31), dtype=torch.int32, device=dev)
+    qres = torch.zeros(4, dtype=torch.int32, device=dev)
+    out = {"decode_rows_per_s": n / (ms / 1e3), "decode_ms": ms,
+           "decode_alg_bytes": 4 * L + 4 * n}
+    for name, lo, hi in (("one_key", 1234, 1234), ("range_1000_keys", 0, 999)):
+        def q():
+            rc = lib.wah_query(bufs.keys.data_ptr(), bufs.offsets.data_ptr(),
+                               bufs.index.data_ptr(), K, L, n, lo, hi, 0, 0, 0,
+                               qwords.data_ptr(), qwords.numel(), qrows.data_ptr(), n,
+                               qres.data_ptr(), qws.data_ptr(), qws_b, sh)
+            assert rc == 0
+        q()
+        qms = time_events(q, 5, torch, stream)
+        r = qres.cpu().numpy()
+        out[name] = {"ms": qms, "rows": int(r[1]), "words": int(r[0])}
+    del rows, qws, qrows, qwords
+    torch.cuda.empty_cache()
+    return out
 
 
 def bench_serving(args, wah, torch, dev):
@@ -472,6 +588,9 @@ def main():
             gbs = alg[p] / (phase_ms[p] / 1e3) / 1e9 if phase_ms[p] > 0 and alg[p] else 0
             print(f"{p}:\t{phase_ms[p] * 1e3:.0f} us\t{gbs:.0f} GB/s", file=sys.stderr)
 
+    decode = None if args.no_decode else bench_decode(args, lib, torch, dev, stream, bufs, n, K, L)
+    ingest = None if args.no_ingest else bench_ingest(args, lib, torch, dev, stream, d_values, n)
+
     # End to end: host values in, host index out, through the public
     # pipelined host-buffer API (wah_pipe_*): every step copies its column in
     # from pinned host memory and its keys/offsets/index out to pinned host
@@ -545,6 +664,8 @@ def main():
             "skewed": skewed,
             "batched": batched,
             "serving": serving,
+            "decode": decode,
+            "ingest": ingest,
             "cpu_baseline": cpu,
         }
         print(json.dumps(line), flush=True)

@@ -324,6 +324,44 @@ int wah_query(const uint32_t* d_keys, const uint32_t* d_offsets,
               uint32_t* d_rows, uint64_t rows_cap, wah_query_result* d_result,
               void* d_workspace, size_t workspace_bytes, void* stream);
 
+/*
+ * Text ingest on the device.  The reference reads its columns from text
+ * files, one value per line, with `while (source >> next)`
+ * (src/cpu.cpp:297-302; files from src/generate_test_data.cpp:45-53).
+ * wah_parse_text parses d_text[0..bytes) (device, 16-byte aligned) the same
+ * way: tokens are separated by whitespace (space, \t \n \v \f \r); a token
+ * of decimal digits whose value fits in 32 bits is a value (leading zeros
+ * allowed; signs are not); parsing stops at the first token that is not
+ * one.  Value i goes to d_values[i] (capacity `capacity`; more values set
+ * WAH_EOVERFLOW, the count stays exact).  d_result (device, 16-byte
+ * aligned) receives the number of values, of tokens, the largest value and
+ * a status.  Workspace: wah_parse_workspace_bytes().  Enqueues on `stream`.
+ */
+typedef struct wah_parse_result {
+  uint64_t values;    /* values parsed (tokens before the first invalid one) */
+  uint64_t tokens;    /* all tokens                                          */
+  uint32_t max_value; /* largest of the values (0 if none)                   */
+  uint32_t status;    /* WAH_OK or WAH_EOVERFLOW                             */
+  uint64_t reserved;
+} wah_parse_result;
+size_t wah_parse_workspace_bytes(void);
+int wah_parse_text(const void* d_text, uint64_t bytes, uint32_t* d_values,
+                   uint64_t capacity, wah_parse_result* d_result,
+                   void* d_workspace, size_t workspace_bytes, void* stream);
+
+/*
+ * Launch-overhead measurements (the reference's overhead_benchmark sends an
+ * empty kernel through the actor facade, src/overhead_benchmark.cpp:64-148,
+ * include/empty_kernel.cl): wah_noop enqueues one empty kernel on `stream`;
+ * a noop graph holds `count` empty kernels captured once into a CUDA graph,
+ * replayed by wah_noop_graph_launch.
+ */
+typedef struct wah_noop_graph wah_noop_graph;
+int wah_noop(void* stream);
+int wah_noop_graph_create(uint32_t count, wah_noop_graph** out);
+int wah_noop_graph_launch(wah_noop_graph* graph, void* stream);
+void wah_noop_graph_destroy(wah_noop_graph* graph);
+
 /* Number of kernels the last wah_build/wah_ctx_build_host on this thread
  * enqueued (launch accounting for benchmarks). */
 uint32_t wah_last_launch_count(void);

@@ -15,6 +15,8 @@ Python face of the C ABI in ``include/wah/wah.h`` (library
                              (src/cpu.cpp:47-74)
 * :func:`decode`             every key's rows on the GPU (row ids, the
                              sorted column, the column itself)
+* :func:`parse_text`         the reference's text data files (one value per
+                             line) parsed on the GPU into a column
 * :func:`query`              rows of a key / value range, or of two ranges
                              combined (OR, AND, AND NOT), as row ids and as
                              a WAH bitmap
@@ -35,7 +37,7 @@ from ._lib import wah_counts
 
 __all__ = ["WahError", "WahIndex", "build_index", "sort_rids_by_value", "build_sorted",
            "HostContext", "Pipeline", "Batch", "Server", "decoded_bitmap", "workspace_bytes", "output_caps",
-           "MAX_ROWS", "last_launch_count", "decode", "query", "QUERY_KEYS", "QUERY_OR",
+           "MAX_ROWS", "last_launch_count", "decode", "query", "parse_text", "QUERY_KEYS", "QUERY_OR",
            "QUERY_AND", "QUERY_ANDNOT"]
 
 MAX_ROWS = 1 << 30
@@ -221,6 +223,49 @@ def decode(idx: WahIndex, n: int, rows: bool = True, values: bool = False,
         raise WahError(st, "wah_decode (device)")
     sizes = {"rows": n, "values": n, "column": n, "key_rows": K}
     return {k: v[:sizes[k]] for k, v in out.items()}
+
+
+class _ParseResult(ctypes.Structure):
+    _fields_ = [("values", ctypes.c_uint64), ("tokens", ctypes.c_uint64),
+                ("max_value", ctypes.c_uint32), ("status", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint64)]
+
+
+def parse_text(data, capacity: int | None = None, stream=None, device="cuda"):
+    """Parses a text data file's bytes (one value per line, or any
+    whitespace between values) on the GPU.
+
+    ``data``: bytes, a numpy uint8 array or a uint8 tensor.  Returns
+    ``(values, info)``: a CUDA int32 tensor (uint32 bits) of the values
+    before the first token that is not a 32-bit decimal number, and a dict
+    with ``values``, ``tokens`` and ``max_value``.  ``capacity`` bounds the
+    values stored (default: one per two bytes, always enough)."""
+    lib = _lib.load()
+    torch = _torch()
+    if isinstance(data, (bytes, bytearray, memoryview)):
+        data = np.frombuffer(bytes(data), dtype=np.uint8)
+    if isinstance(data, np.ndarray):
+        arr = np.ascontiguousarray(data, dtype=np.uint8)
+        if not arr.flags.writeable:
+            arr = arr.copy()
+        t = torch.from_numpy(arr).to(device)
+    else:
+        t = data.to(device).contiguous()
+    nbytes = t.numel()
+    cap = (nbytes + 1) // 2 if capacity is None else int(capacity)
+    out = torch.empty(max(cap, 1), dtype=torch.int32, device=t.device)
+    res = torch.zeros(4, dtype=torch.int64, device=t.device)
+    wsb = int(lib.wah_parse_workspace_bytes())
+    ws = torch.empty(wsb, dtype=torch.uint8, device=t.device)
+    text_ptr = t.data_ptr() if nbytes else ws.data_ptr()
+    rc = lib.wah_parse_text(text_ptr, nbytes, out.data_ptr(), cap, res.data_ptr(),
+                            ws.data_ptr(), wsb, _stream_handle(stream))
+    _check(rc, "wah_parse_text")
+    r = _ParseResult.from_buffer_copy(res.cpu().numpy().tobytes())
+    if r.status != WAH_OK:
+        raise WahError(int(r.status), "wah_parse_text (device)")
+    info = {"values": int(r.values), "tokens": int(r.tokens), "max_value": int(r.max_value)}
+    return out[:int(r.values)], info
 
 
 def _term(t):

@@ -20,7 +20,7 @@ OBJ_DIR = os.path.join(PKG_DIR, "_build")
 LIB_PATH = os.path.join(PKG_DIR, "libwah_gb300.so")
 
 CUDA_SOURCES = ["wah_sort.cu", "wah_index.cu", "wah_api.cu", "wah_batch.cu", "wah_pipe.cu",
-                "wah_serve.cu", "wah_noalloc.cu", "wah_query.cu"]
+                "wah_serve.cu", "wah_noalloc.cu", "wah_query.cu", "wah_ingest.cu"]
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo",
               "-std=c++17", "-Xcompiler", "-fPIC", "-I" + INCLUDE, "-I" + CSRC]
 
@@ -63,8 +63,8 @@ def build(verbose: bool = False) -> str:
 HOST_DIR = os.path.join(PKG_DIR, "host")
 BIN_DIR = os.path.join(PKG_DIR, "bin")
 # host programs: (source, links libwah_gb300.so)
-HOST_PROGRAMS = [("phases.cpp", True), ("gpu.cpp", True), ("generate.cpp", False),
-                 ("actors_test.cpp", False)]
+HOST_PROGRAMS = [("phases.cpp", True), ("gpu.cpp", True), ("overhead.cpp", True),
+                 ("generate.cpp", False), ("actors_test.cpp", False)]
 CXX_FLAGS = ["-O2", "-std=c++17", "-pthread", "-Wall", "-Wextra", "-I" + INCLUDE]
 
 
@@ -175,6 +175,12 @@ SIGNATURES = {
     "wah_query_workspace_bytes": ([_u64], ctypes.c_size_t),
     "wah_query": ([_vp, _vp, _vp, _u32, _u32, _u64, _u32, _u32, ctypes.c_int, _u32, _u32,
                    _vp, _u64, _vp, _u64, _vp, _vp, ctypes.c_size_t, _vp], ctypes.c_int),
+    "wah_parse_workspace_bytes": ([], ctypes.c_size_t),
+    "wah_parse_text": ([_vp, _u64, _vp, _u64, _vp, _vp, ctypes.c_size_t, _vp], ctypes.c_int),
+    "wah_noop": ([_vp], ctypes.c_int),
+    "wah_noop_graph_create": ([_u32, ctypes.POINTER(_vp)], ctypes.c_int),
+    "wah_noop_graph_launch": ([_vp, _vp], ctypes.c_int),
+    "wah_noop_graph_destroy": ([_vp], None),
     "wah_last_launch_count": ([], _u32),
     "wah_device_count": ([], ctypes.c_int),
     "wah_device_name": ([ctypes.c_int, ctypes.c_char_p, ctypes.c_size_t], ctypes.c_int),

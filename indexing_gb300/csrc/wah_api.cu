@@ -449,3 +449,59 @@ void wah_stream_destroy(void* stream) {
 }
 
 }  // extern "C"
+
+namespace wah {
+// The empty kernel of the launch-overhead measurements.
+__global__ void k_noop() {}
+}  // namespace wah
+
+struct wah_noop_graph {
+  cudaGraphExec_t exec = nullptr;
+  cudaStream_t capture = nullptr;
+};
+
+extern "C" {
+
+int wah_noop(void* stream) {
+  k_noop<<<1, 32, 0, static_cast<cudaStream_t>(stream)>>>();
+  *last_launches_slot() = 1;
+  return cuda_status(cudaGetLastError());
+}
+
+void wah_noop_graph_destroy(wah_noop_graph* g) {
+  if (!g) return;
+  if (g->exec) cudaGraphExecDestroy(g->exec);
+  if (g->capture) cudaStreamDestroy(g->capture);
+  delete g;
+}
+
+int wah_noop_graph_create(uint32_t count, wah_noop_graph** out) {
+  if (!out || count == 0) return WAH_EINVAL;
+  *out = nullptr;
+  wah_noop_graph* g = new (std::nothrow) wah_noop_graph;
+  if (!g) return WAH_ENOMEM;
+  cudaError_t e = cudaStreamCreateWithFlags(&g->capture, cudaStreamNonBlocking);
+  cudaGraph_t graph = nullptr;
+  if (e == cudaSuccess) e = cudaStreamBeginCapture(g->capture, cudaStreamCaptureModeThreadLocal);
+  if (e == cudaSuccess) {
+    for (uint32_t i = 0; i < count; ++i) k_noop<<<1, 32, 0, g->capture>>>();
+    const cudaError_t le = cudaGetLastError();
+    e = cudaStreamEndCapture(g->capture, &graph);
+    if (e == cudaSuccess) e = le;
+  }
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&g->exec, graph, 0);
+  if (graph) cudaGraphDestroy(graph);
+  if (e != cudaSuccess) {
+    wah_noop_graph_destroy(g);
+    return cuda_status(e);
+  }
+  *out = g;
+  return WAH_OK;
+}
+
+int wah_noop_graph_launch(wah_noop_graph* g, void* stream) {
+  if (!g) return WAH_EINVAL;
+  return cuda_status(cudaGraphLaunch(g->exec, static_cast<cudaStream_t>(stream)));
+}
+
+}  // extern "C"

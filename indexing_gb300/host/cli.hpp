@@ -148,6 +148,56 @@ inline bool read_values(const std::string& path, std::vector<uint32_t>* out) {
   return true;
 }
 
+// The same reading on the device: the file's bytes are copied to the GPU
+// and parsed there by wah_parse_text (same rule as read_values), then the
+// values come back.  Returns false with a message in *err on failure.
+inline bool read_values_gpu(const std::string& path, std::vector<uint32_t>* out,
+                            std::string* err) {
+  FILE* f = std::fopen(path.c_str(), "rb");
+  if (!f) {
+    *err = "cannot open '" + path + "'";
+    return false;
+  }
+  std::fseek(f, 0, SEEK_END);
+  const long len = std::ftell(f);
+  std::fseek(f, 0, SEEK_SET);
+  const uint64_t bytes = len > 0 ? static_cast<uint64_t>(len) : 0;
+  const uint64_t cap = (bytes + 1) / 2;
+  void *h_text = nullptr, *d_text = nullptr, *d_vals = nullptr, *d_res = nullptr, *d_ws = nullptr,
+       *stream = nullptr;
+  const size_t ws_bytes = wah_parse_workspace_bytes();
+  int rc = wah_host_alloc(bytes ? bytes : 1, &h_text);
+  if (rc == WAH_OK && bytes && std::fread(h_text, 1, bytes, f) != bytes) rc = WAH_EINVAL;
+  std::fclose(f);
+  if (rc == WAH_OK) rc = wah_dev_alloc((bytes + 16) & ~uint64_t(15), &d_text);
+  if (rc == WAH_OK) rc = wah_dev_alloc((cap ? cap : 1) * 4, &d_vals);
+  if (rc == WAH_OK) rc = wah_dev_alloc(sizeof(wah_parse_result), &d_res);
+  if (rc == WAH_OK) rc = wah_dev_alloc(ws_bytes, &d_ws);
+  if (rc == WAH_OK) rc = wah_stream_create(&stream);
+  if (rc == WAH_OK && bytes) rc = wah_copy(d_text, h_text, bytes, stream);
+  if (rc == WAH_OK)
+    rc = wah_parse_text(d_text, bytes, static_cast<uint32_t*>(d_vals), cap,
+                        static_cast<wah_parse_result*>(d_res), d_ws, ws_bytes, stream);
+  wah_parse_result res{};
+  if (rc == WAH_OK) rc = wah_copy(&res, d_res, sizeof res, stream);
+  if (rc == WAH_OK) rc = wah_stream_sync(stream);
+  if (rc == WAH_OK) rc = static_cast<int>(res.status);
+  if (rc == WAH_OK) {
+    out->resize(res.values);
+    if (res.values) rc = wah_copy(out->data(), d_vals, res.values * 4, stream);
+    if (rc == WAH_OK) rc = wah_stream_sync(stream);
+  }
+  if (stream) wah_stream_destroy(stream);
+  for (void* p : {d_text, d_vals, d_res, d_ws})
+    if (p) wah_dev_free(p);
+  if (h_text) wah_host_free(h_text);
+  if (rc != WAH_OK) {
+    *err = std::string("parsing '") + path + "' on the GPU: " + wah_strerror(rc);
+    return false;
+  }
+  return true;
+}
+
 // The reference's built-in 32-value fixture (src/cpu.cpp:292-295).
 inline std::vector<uint32_t> builtin_values() {
   return {10, 7, 22, 6, 7, 1, 9, 42, 2, 5, 13, 3, 2, 1, 0, 1,

@@ -19,7 +19,8 @@
 // default 1023 = 33 x 31).
 //
 // Flags as the reference (-f, -b bound, -d device name, -p print,
-// --batch-size, -j/--jobs, -w/--work-groups) plus --output FILE.  Prints the
+// --batch-size, -j/--jobs, -w/--work-groups) plus --output FILE and
+// --host-parse (the data file is parsed on the GPU by default).  Prints the
 // reference's lines ('N' values, maximum value, device, -p listing of keys
 // 0..bound, Time: 'X' ms).
 #include <algorithm>
@@ -453,7 +454,7 @@ behavior indexer(actor_ctx<indexer_state>& self) {
 int main(int argc, char** argv) {
   std::string filename, device_name, output;
   uint32_t bound = 0, batch_size = 1023, jobs = 1, work_groups = 1;
-  bool print_results = false;
+  bool print_results = false, host_parse = false;
   const std::vector<wahcli::flag> flags = {
       {"data-file", 'f', "file with test data (one value per line)", wahcli::flag::STRING, &filename},
       {"bound", 'b', "maximum value (0 will scan values)", wahcli::flag::U32, &bound},
@@ -466,6 +467,8 @@ int main(int argc, char** argv) {
       {"jobs", 'j', "batches in flight on the GPU (1; 0 = 4, at most 8)", wahcli::flag::U32, &jobs},
       {"output", 'o', "write K, L, keys, offsets, index (u32) to this file", wahcli::flag::STRING,
        &output},
+      {"host-parse", 0, "parse the data file on the host instead of the GPU", wahcli::flag::BOOL,
+       &host_parse},
   };
   const int pf = wahcli::parse_flags(argc, argv, flags);
   if (pf != 0) return pf > 0 ? 0 : 2;
@@ -475,8 +478,11 @@ int main(int argc, char** argv) {
   } else {
     std::printf("Reading data from '%s' ... ", filename.c_str());
     std::fflush(stdout);
-    if (!wahcli::read_values(filename, &values)) {
-      std::fprintf(stderr, "cannot read '%s'\n", filename.c_str());
+    std::string err;
+    if (host_parse ? !wahcli::read_values(filename, &values)
+                   : !wahcli::read_values_gpu(filename, &values, &err)) {
+      std::fprintf(stderr, "%s\n", err.empty() ? ("cannot read '" + filename + "'").c_str()
+                                                : err.c_str());
       return 2;
     }
   }

@@ -14,8 +14,10 @@
 //   Total
 //
 // Flags as the reference (-f data file, -b bound, -d device name, -p print)
-// plus --describe (label each line, the reference's WITH_DESCRIPTION build)
-// and --output FILE (binary result: K, L, keys, offsets, index).  Unlike the
+// plus --describe (label each line, the reference's WITH_DESCRIPTION build),
+// --output FILE (binary result: K, L, keys, offsets, index) and --host-parse
+// (read the data file on the host; by default its bytes are parsed on the
+// GPU by wah_parse_text, before the timed phases as in the reference).  Unlike the
 // reference, -p prints the index as the cpu program does, and the keys are
 // produced (the reference's phases never materialises them).
 #include <algorithm>
@@ -153,7 +155,7 @@ behavior device_actor(actor_ctx<device_state>& self) {
 int main(int argc, char** argv) {
   std::string filename, device_name, output;
   uint32_t bound = 0;
-  bool print_results = false, describe = false;
+  bool print_results = false, describe = false, host_parse = false;
   const std::vector<wahcli::flag> flags = {
       {"data-file", 'f', "file with test data (one value per line)", wahcli::flag::STRING, &filename},
       {"bound", 'b', "maximum value (0 will scan values)", wahcli::flag::U32, &bound},
@@ -161,6 +163,8 @@ int main(int argc, char** argv) {
        wahcli::flag::STRING, &device_name},
       {"print", 'p', "print resulting bitmap index", wahcli::flag::BOOL, &print_results},
       {"describe", 0, "label each timing line", wahcli::flag::BOOL, &describe},
+      {"host-parse", 0, "parse the data file on the host instead of the GPU", wahcli::flag::BOOL,
+       &host_parse},
       {"output", 'o', "write K, L, keys, offsets, index (u32) to this file", wahcli::flag::STRING,
        &output},
   };
@@ -170,12 +174,6 @@ int main(int argc, char** argv) {
     std::printf("A filename with test data is required, see --help for details.\n");
     return 2;
   }
-  std::vector<uint32_t> values;
-  if (!wahcli::read_values(filename, &values)) {
-    std::fprintf(stderr, "cannot read '%s'\n", filename.c_str());
-    return 2;
-  }
-  if (bound == 0 && !values.empty()) bound = *std::max_element(values.begin(), values.end());
   const int dev = wahcli::find_device(device_name, true);
   if (dev < 0) {
     std::fprintf(stderr, "No device found.\n");
@@ -185,6 +183,16 @@ int main(int argc, char** argv) {
     std::fprintf(stderr, "cannot select device %d\n", dev);
     return 3;
   }
+  // reading the file is not timed (the reference reads it before its clock)
+  std::vector<uint32_t> values;
+  std::string err;
+  if (host_parse ? !wahcli::read_values(filename, &values)
+                 : !wahcli::read_values_gpu(filename, &values, &err)) {
+    std::fprintf(stderr, "%s\n", err.empty() ? ("cannot read '" + filename + "'").c_str()
+                                              : err.c_str());
+    return 2;
+  }
+  if (bound == 0 && !values.empty()) bound = *std::max_element(values.begin(), values.end());
 
   auto line = [&](const char* label, uint64_t us) {
     if (describe)

@@ -182,3 +182,47 @@ def test_generate_then_phases_and_gpu(progs, tmp_path):
     assert r.returncode == 0, r.stderr
     assert_matches_oracle(a, v, "phases generated")
     assert_matches_oracle(b, v, "gpu generated")
+
+
+def test_gpu_and_host_parsing_agree(progs, tmp_path):
+    """The data file read on the GPU (default) and on the host (--host-parse)
+    gives the same column: separators of every kind, leading zeros, and a
+    token that ends the stream."""
+    rng = np.random.default_rng(21)
+    parts = []
+    for i in range(30_000):
+        parts.append(("0" * int(i % 3)) + str(int(rng.integers(0, 70_000))))
+        parts.append(["\n", "\r\n", " ", "\t", "  \n"][i % 5])
+    parts.insert(40_001, "oops ")
+    data = tmp_path / "v.txt"
+    data.write_text("".join(parts))
+    a, b = tmp_path / "a.bin", tmp_path / "b.bin"
+    ra = run([progs["phases"], "-f", str(data), "-o", str(a)])
+    rb = run([progs["phases"], "-f", str(data), "-o", str(b), "--host-parse"])
+    assert ra.returncode == 0 and rb.returncode == 0, ra.stderr + rb.stderr
+    assert a.read_bytes() == b.read_bytes()
+    # "oops" is glued to value 20,001, so that token ends the stream: the
+    # column is the first 20,000 values
+    v = np.array([int(x) for x in "".join(parts[:40_000]).split()], dtype=np.uint32)
+    assert v.size == 20_000
+    assert_matches_oracle(a, v, "phases parsed")
+
+
+def test_overhead_program(tmp_path):
+    """The launch-overhead program runs and reports every figure."""
+    import json
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    _lib.build()
+    prog = _lib.build_host(["overhead"])["overhead"]
+    r = run([prog, "-i", "200", "-k", "500", "--rows", "4096", "--columns", "64"])
+    assert r.returncode == 0, r.stderr
+    lines = r.stdout.splitlines()
+    assert lines[0].startswith("Took ") and lines[0].endswith(" runs.")
+    d = json.loads(lines[1])
+    for k in ("actor_us", "direct_us", "build_us"):
+        assert d[k]["mean"] > 0
+    assert d["stream_us_per_launch"] > 0 and d["graph_us_per_launch"] > 0
+    assert d["build_us"]["launches"] >= 5
+    assert d["batched_us_per_column"] > 0
