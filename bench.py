@@ -64,6 +64,9 @@ def parse():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--batch-cols", type=int, default=4096)
     ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="skip timing every radix tile shape on this size before the run")
+    ap.add_argument("--tune-cache", default=None, help="autotuner cache file")
     ap.add_argument("--no-ingest", action="store_true")
     ap.add_argument("--no-decode", action="store_true")
     ap.add_argument("--serve-requests", type=int, default=20000)
@@ -501,6 +504,10 @@ def main():
             raise SystemExit(f"unsupported --sort-items {args.sort_items}")
     n, card = args.n, args.card
     bound = card - 1
+    tuned = None
+    if not args.no_autotune and not args.sort_items:
+        t, cached = wah.autotune(n, bound, args.tune_cache)
+        tuned = {"tuning": t, "from_cache": cached}
     values_np = gen_uniform(n, card, args.seed + rank)
     d_values = torch.from_numpy(values_np.view(np.int32)).to(dev)
     bufs = wah._Buffers(n, bound, dev)
@@ -653,6 +660,7 @@ def main():
                        "l2": "inputs larger than L2 (1 GiB column), no flush"},
             "outputs": {"keycnt": K, "index_len": L, "merged": k},
             "sort_items": int(lib.wah_get_tuning()),
+            "autotune": tuned,
             "hbm_gbs_pipeline": total_alg / (ms_per_step / 1e3) / 1e9,
             "phase_us": {p: round(phase_ms[p] * 1e3, 1) for p in PHASES},
             "roofline": {"bound": "hbm", "kernel": dom, "per_unit": per_unit.get(dom),

@@ -378,6 +378,19 @@ int wah_set_tuning(int sort_items);
 int wah_get_tuning(void);
 
 /*
+ * Autotuner: times every tile shape wah_set_tuning accepts on a synthetic
+ * column of n rows with values up to bound (the reference's radix shape is
+ * fixed, src/phases.cpp:445-453; its radix test program takes it as flags,
+ * src/radix.cpp:161-184), applies the fastest, and appends it to the text
+ * file cache_path (NULL: no cache) under the key (device name, floor(log2 n),
+ * digit passes).  When the cache already holds the key, its entry is applied
+ * without timing and *from_cache is 1.  Allocates and frees its own device
+ * memory; synchronises.  *chosen receives the tuning applied.
+ */
+int wah_autotune(uint64_t n, uint32_t bound, const char* cache_path, int* chosen,
+                 int* from_cache);
+
+/*
  * Per-phase device timing, the counterpart of the reference's
  * SHOW_TIME_CONSUMPTION "N us" lines (src/phases.cpp:714-1127), measured with
  * CUDA events on the build's own stream instead of host clocks around

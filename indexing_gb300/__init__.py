@@ -37,7 +37,7 @@ from ._lib import wah_counts
 
 __all__ = ["WahError", "WahIndex", "build_index", "sort_rids_by_value", "build_sorted",
            "HostContext", "Pipeline", "Batch", "Server", "decoded_bitmap", "workspace_bytes", "output_caps",
-           "MAX_ROWS", "last_launch_count", "decode", "query", "parse_text", "QUERY_KEYS", "QUERY_OR",
+           "MAX_ROWS", "last_launch_count", "autotune", "decode", "query", "parse_text", "QUERY_KEYS", "QUERY_OR",
            "QUERY_AND", "QUERY_ANDNOT"]
 
 MAX_ROWS = 1 << 30
@@ -106,6 +106,19 @@ def last_launch_count() -> int:
 def _torch():
     import torch
     return torch
+
+
+def autotune(n: int, bound: int = 0, cache_path: str | None = None):
+    """Times every radix tile shape on a synthetic column of n rows (values
+    up to bound), applies the fastest process-wide, and caches the choice per
+    (device, size bucket, digit passes) in ``cache_path``.  Returns
+    ``(tuning, from_cache)``."""
+    lib = _lib.load()
+    chosen, cached = ctypes.c_int(), ctypes.c_int()
+    rc = lib.wah_autotune(n, bound, cache_path.encode() if cache_path else None,
+                          ctypes.byref(chosen), ctypes.byref(cached))
+    _check(rc, "wah_autotune")
+    return chosen.value, bool(cached.value)
 
 
 def _stream_handle(stream) -> int:

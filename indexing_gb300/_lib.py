@@ -20,7 +20,8 @@ OBJ_DIR = os.path.join(PKG_DIR, "_build")
 LIB_PATH = os.path.join(PKG_DIR, "libwah_gb300.so")
 
 CUDA_SOURCES = ["wah_sort.cu", "wah_index.cu", "wah_api.cu", "wah_batch.cu", "wah_pipe.cu",
-                "wah_serve.cu", "wah_noalloc.cu", "wah_query.cu", "wah_ingest.cu"]
+                "wah_serve.cu", "wah_noalloc.cu", "wah_query.cu", "wah_ingest.cu",
+                "wah_tune.cu"]
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo",
               "-std=c++17", "-Xcompiler", "-fPIC", "-I" + INCLUDE, "-I" + CSRC]
 
@@ -195,6 +196,8 @@ SIGNATURES = {
     "wah_stream_destroy": ([_vp], None),
     "wah_set_tuning": ([ctypes.c_int], ctypes.c_int),
     "wah_get_tuning": ([], ctypes.c_int),
+    "wah_autotune": ([_u64, _u32, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int),
+                      ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
     "wah_events_create": ([_u32, ctypes.POINTER(_vp)], ctypes.c_int),
     "wah_events_destroy": ([_u32, ctypes.POINTER(_vp)], None),
     "wah_events_elapsed": ([_vp, _vp, ctypes.POINTER(ctypes.c_float)], ctypes.c_int),
