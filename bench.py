@@ -151,6 +151,22 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def replica_throughput(elapsed_ms: float, rows_per_step: int, steps: int, dist=None,
+                       device="cpu"):
+    """Replicas only: every rank builds its own column, no collective on the
+    data path.  The job's time is the slowest rank's (max over ranks); the
+    job's throughput counts every rank's rows.  Returns (max_ms, rows/s)."""
+    import torch
+    world = 1
+    max_ms = elapsed_ms
+    if dist is not None and dist.is_initialized():
+        world = dist.get_world_size()
+        t = torch.tensor([elapsed_ms], device=device, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        max_ms = float(t.item())
+    return max_ms, world * rows_per_step * steps / (max_ms / 1e3)
+
+
 def time_events(fn, steps, torch, stream):
     """Mean ms of fn() over steps, CUDA events on `stream`."""
     a = torch.cuda.Event(enable_timing=True)
@@ -571,13 +587,8 @@ def main():
     for arr in ev_arrays:
         lib.wah_events_destroy(n_ev, arr)
 
-    max_ms = elapsed_ms
-    if dist:
-        t = torch.tensor([elapsed_ms], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        max_ms = float(t.item())
+    max_ms, value = replica_throughput(elapsed_ms, n, args.steps, dist, dev)
     ms_per_step = max_ms / args.steps
-    value = world * n * args.steps / (max_ms / 1e3)
 
     # Algorithmic bytes (per build; integer keys <= 16 bits -> 2 digit passes):
     #   histogram 4n, pass0 12n (read key, write key+rid), pass1 16n,
