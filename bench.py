@@ -593,9 +593,14 @@ def main():
     # Algorithmic bytes (per build; integer keys <= 16 bits -> 2 digit passes):
     #   histogram 4n, pass0 12n (read key, write key+rid), pass1 16n,
     #   build 8n + 4L + 8K (read sorted key+rid, write words, keys, offsets)
+    # DRAM bytes per row of each phase's kernels (dram__bytes_read.sum +
+    # dram__bytes_write.sum, one ncu capture of a 67,108,864-row uniform
+    # 16-bit column with the same tile shape); traffic grows with rows.
+    traffic_per_row = {"histogram": 4.05, "pass0": 15.18, "pass1": 23.30, "build": 23.33}
     alg = {"histogram": 4 * n, "plan": 0, "pass0": 12 * n, "pass1": 16 * n, "pass2": 0,
            "pass3": 0, "build": 8 * n + 4 * L + 8 * K}
-    per_unit = {"histogram": "4 B/row", "pass0": "12 B/row", "pass1": "16 B/row",
+    per_unit = {"histogram": "4 B/row", "pass0": "12 B/row",
+                "pass1": "16 B/row (range count + scan + scatter timed together)",
                 "build": "8 B/row + 4 B/word + 8 B/key"}
     dom = max(PHASES, key=lambda p: phase_ms[p])
     peak, peak_kind = load_peaks()
@@ -676,7 +681,10 @@ def main():
             "phase_us": {p: round(phase_ms[p] * 1e3, 1) for p in PHASES},
             "roofline": {"bound": "hbm", "kernel": dom, "per_unit": per_unit.get(dom),
                          "achieved": ach, "peak": peak, "unit": "GB/s",
-                         "frac": ach / peak, "peak_kind": peak_kind, "traffic": None},
+                         "frac": ach / peak, "peak_kind": peak_kind,
+                         "traffic": (traffic_per_row[dom] * n
+                                     if card == 65536 and dom in traffic_per_row else None),
+                         "traffic_source": "ncu capture at 67,108,864 rows, scaled by rows"},
             "gpu_launches": launches,
             "clocks": cl,
             "e2e": e2e,
