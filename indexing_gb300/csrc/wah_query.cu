@@ -705,7 +705,7 @@ constexpr size_t kAlign = 256;
 size_t align_up(size_t x) { return (x + kAlign - 1) / kAlign * kAlign; }
 
 uint32_t query_ranges() {
-  const uint32_t r = (uint32_t)sm_count_current() * 2;
+  const uint32_t r = (uint32_t)sm_count_current() * 8;
   return r < kMaxQueryRanges ? r : kMaxQueryRanges;
 }
 

@@ -357,13 +357,17 @@ __global__ void __launch_bounds__(kSortThreads, 2)
     uint32_t key[ITEMS];
     if (valid == TILE) {
       // phases of each buffer's barrier complete in turn; the parity of the
-      // next one is tracked per buffer (a tile read with plain loads uses none)
-      const bool ok = mbar_wait_bounded(&sm.bar[cur], (phase_bits >> cur) & 1u);
-      phase_bits ^= 1u << cur;
-      if (!ok) {
+      // next one is tracked per buffer (a tile read with plain loads uses
+      // none).  One thread waits for the copy; the block barrier then hands
+      // its completion (and the zeroed counters) to every thread.
+      if (tid == 0 && !mbar_wait_bounded(&sm.bar[cur], (phase_bits >> cur) & 1u)) {
         set_status(status, WAH_ETIMEOUT);
         sm.abort = 1;
       }
+      phase_bits ^= 1u << cur;
+    }
+    __syncthreads();
+    if (valid == TILE) {
       const uint32_t* kp = sm.in_keys[cur] + row0;
 #pragma unroll
       for (int j = 0; j < ITEMS; ++j) key[j] = kp[j * 32];
@@ -379,7 +383,6 @@ __global__ void __launch_bounds__(kSortThreads, 2)
         if (rin) sm.in_rids[cur][r] = r < valid ? rin[base + r] : 0u;
       }
     }
-    __syncthreads();
 
     // Peer masks (independent), then two interleaved counter chains.
     uint32_t rank[ITEMS];
