@@ -23,7 +23,8 @@
 // values[i].  A token of up to 16 characters is converted eight digits at a
 // time in 64-bit registers (SWAR); longer ones (leading zeros) character by
 // character.  Invalid tokens lower a device-wide "first invalid token" with
-// atomicMin; the largest value of the tokens before it is reduced at the end.
+// atomicMin.  The largest value is reduced while parsing; only when an
+// invalid token cuts the column is it recomputed over the values before it.
 #include "wah_common.cuh"
 
 namespace wah {
@@ -37,9 +38,10 @@ constexpr uint64_t kNoInvalid = ~0ull;
 struct ParseCtrl {
   unsigned long long first_invalid;  // token number, kNoInvalid if none
   unsigned long long tokens;         // all tokens
-  uint32_t max_value;
-  uint32_t done_blocks;  // k_parse_finish blocks that have finished
-  uint32_t pad[2];
+  uint32_t max_value;       // over every valid token (k_parse_emit)
+  uint32_t done_blocks;     // k_parse_finish blocks that have finished
+  uint32_t recomputed_max;  // over the tokens before the first invalid one
+  uint32_t pad;
 };
 
 struct ParseRange {
@@ -47,27 +49,32 @@ struct ParseRange {
   unsigned long long base;    // tokens before the range (scan)
 };
 
-// 0xFF in each byte of w that is whitespace (space, \t..\r), else 0x00.
-__device__ __forceinline__ uint32_t ws_bytes4(uint32_t w) {
-  const uint32_t sp = __vcmpeq4(w, 0x20202020u);
-  const uint32_t ctl = __vcmpgeu4(w, 0x09090909u) & __vcmpleu4(w, 0x0d0d0d0du);
-  return sp | ctl;
+// Bit 7 of each byte of x set where the byte is whitespace (space, \t..\r),
+// exactly, with carry-free byte arithmetic (SWAR): bytes in [9, 13] are
+// those >= 9 and not >= 14 among bytes below 0x80; spaces are the zero bytes
+// of x ^ 0x20202020.
+__device__ __forceinline__ uint32_t ws_flags4(uint32_t x) {
+  const uint32_t lo = x & 0x7F7F7F7Fu;
+  const uint32_t ge9 = (lo + 0x77777777u) & 0x80808080u;
+  const uint32_t ge14 = (lo + 0x72727272u) & 0x80808080u;
+  const uint32_t ctl = ge9 & ~ge14 & ~x & 0x80808080u;
+  const uint32_t y = x ^ 0x20202020u;
+  const uint32_t sp = ~(((y & 0x7F7F7F7Fu) + 0x7F7F7F7Fu) | y) & 0x80808080u;
+  return ctl | sp;
 }
 
 // One bit per byte (bit i = byte i) of the 16 bytes in q that are not
-// whitespace.
+// whitespace: each word's four byte flags are gathered into four bits by
+// one multiply (the partial products land on distinct bits).
 __device__ __forceinline__ uint32_t nonws_mask16(uint4 q) {
-  uint32_t m = 0;
   const uint32_t w[4] = {q.x, q.y, q.z, q.w};
+  uint32_t m = 0;
 #pragma unroll
   for (int k = 0; k < 4; ++k) {
-    const uint32_t ws = ws_bytes4(w[k]);
-    // compress the 4 byte flags to 4 bits: one bit per byte
-    const uint32_t b =
-        ((ws >> 7) & 1u) | ((ws >> 14) & 2u) | ((ws >> 21) & 4u) | ((ws >> 28) & 8u);
-    m |= (~b & 0xFu) << (4 * k);
+    const uint32_t f = (ws_flags4(w[k]) >> 7) & 0x01010101u;
+    m |= ((f * 0x10204080u) >> 28) << (4 * k);
   }
-  return m;
+  return ~m & 0xFFFFu;
 }
 
 __device__ __forceinline__ bool is_ws(uint32_t c) { return c == 0x20u || (c >= 9u && c <= 13u); }
@@ -141,6 +148,7 @@ __global__ void __launch_bounds__(kPScanThreads) k_parse_scan(ParseRange* rng, u
     ctrl->first_invalid = kNoInvalid;
     ctrl->max_value = 0;
     ctrl->done_blocks = 0;
+    ctrl->recomputed_max = 0;
   }
 }
 
@@ -200,12 +208,15 @@ __device__ __forceinline__ bool swar_digits(uint64_t x, uint32_t len, uint64_t* 
 __global__ void __launch_bounds__(kPThreads) k_parse_emit(ParseIn in, const ParseRange* rng,
                                                           uint32_t* values, uint64_t cap,
                                                           ParseCtrl* ctrl) {
-  __shared__ uint64_t s_w[kPThreads / 32 + 1];
+  __shared__ uint32_t s_w[kPThreads / 32 + 1];
+  __shared__ uint32_t s_max[kPThreads / 32];
   __shared__ __align__(16) unsigned char s_text[kPWindow];
   const uint64_t lo = (uint64_t)blockIdx.x * in.range_bytes;
   const uint64_t hi = lo + in.range_bytes < in.bytes ? lo + in.range_bytes : in.bytes;
   if (lo >= hi) return;
+  const uint32_t lane = threadIdx.x & 31;
   uint64_t carry = rng[blockIdx.x].base;
+  uint32_t vmax = 0;
   for (uint64_t s = lo; s < hi; s += kPStep) {
     const uint64_t p = s + threadIdx.x * 16ull;
     // bytes past the range are loaded too (whitespace past the text's end)
@@ -214,24 +225,28 @@ __global__ void __launch_bounds__(kPThreads) k_parse_emit(ParseIn in, const Pars
     if (threadIdx.x < 4)
       reinterpret_cast<uint4*>(s_text + kPStep)[threadIdx.x] =
           load16(in, s + kPStep + 16ull * threadIdx.x);
+    const uint32_t nw = nonws_mask16(q);
+    // the next 16 bytes' mask: the next lane's, or (last lane) computed here
+    uint32_t nw_next = __shfl_down_sync(0xffffffffu, nw, 1);
+    const uint32_t prev_last = __shfl_up_sync(0xffffffffu, nw >> 15, 1);
     __syncthreads();
-    uint32_t st = 0, nw32 = 0;
+    if (lane == 31)
+      nw_next = nonws_mask16(reinterpret_cast<const uint4*>(s_text)[threadIdx.x + 1]);
+    uint32_t st = 0;
     if (p < hi) {
-      const uint32_t nw = nonws_mask16(q);
       uint32_t prev_nonws;
-      if (threadIdx.x > 0)
+      if (lane > 0)
+        prev_nonws = prev_last & 1u;
+      else if (threadIdx.x > 0)
         prev_nonws = !is_ws(s_text[threadIdx.x * 16 - 1]);
       else
         prev_nonws = p > 0 && !is_ws(in.text[p - 1]);
       st = nw & ~((nw << 1) | prev_nonws) & 0xFFFFu;
-      if (st) {
-        const uint4 q2 = reinterpret_cast<const uint4*>(s_text)[threadIdx.x + 1];
-        nw32 = nw | (nonws_mask16(q2) << 16);
-      }
     }
-    uint64_t tot;
-    const uint64_t ex = block_exclusive_scan64<kPThreads>(__popc(st), &tot, s_w);
+    uint32_t tot;
+    const uint32_t ex = block_exclusive_scan<kPThreads>(__popc(st), &tot, s_w);
     uint64_t idx = carry + ex;
+    const uint32_t nw32 = nw | (nw_next << 16);
     uint32_t m = st;
     while (m) {
       const uint32_t b = __ffs(m) - 1;
@@ -257,6 +272,7 @@ __global__ void __launch_bounds__(kPThreads) k_parse_emit(ParseIn in, const Pars
       }
       if (ok) {
         if (idx < cap) values[idx] = (uint32_t)v;
+        vmax = (uint32_t)v > vmax ? (uint32_t)v : vmax;
       } else {
         atomicMin(&ctrl->first_invalid, (unsigned long long)idx);
       }
@@ -265,22 +281,48 @@ __global__ void __launch_bounds__(kPThreads) k_parse_emit(ParseIn in, const Pars
     carry += tot;
     __syncthreads();  // s_text is rewritten by the next step
   }
+  // largest value of every valid token (k_parse_finish redoes it over the
+  // tokens before the first invalid one when there is one)
+  vmax = __reduce_max_sync(0xffffffffu, vmax);
+  if (lane == 0) s_max[threadIdx.x >> 5] = vmax;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    uint32_t b = 0;
+    for (int w = 0; w < kPThreads / 32; ++w) b = s_max[w] > b ? s_max[w] : b;
+    atomicMax(&ctrl->max_value, b);
+  }
 }
 
-// Largest value among the tokens before the first invalid one, and the
-// result record (written by the last block to finish).
+// The result record.  Without an invalid token the largest value is the one
+// k_parse_emit reduced; otherwise it is recomputed over the values before the
+// first invalid token (four 16-byte loads in flight per thread).
 __global__ void __launch_bounds__(kPThreads) k_parse_finish(const uint32_t* values, uint64_t cap,
                                                             ParseCtrl* ctrl,
                                                             wah_parse_result* res) {
   __shared__ uint32_t s_max[kPThreads / 32];
   const uint64_t fi = ctrl->first_invalid;
   const uint64_t count = ctrl->tokens < fi ? ctrl->tokens : fi;
-  const uint64_t stored = count < cap ? count : cap;
+  const bool recompute = fi != kNoInvalid;
   uint32_t m = 0;
-  for (uint64_t i = (uint64_t)blockIdx.x * kPThreads + threadIdx.x; i < stored;
-       i += (uint64_t)gridDim.x * kPThreads) {
-    const uint32_t v = values[i];
-    m = v > m ? v : m;
+  if (recompute) {
+    const uint64_t stored = count < cap ? count : cap;
+    const uint64_t n4 = stored / 4;
+    const uint4* v4 = reinterpret_cast<const uint4*>(values);
+    const uint64_t stride = (uint64_t)gridDim.x * kPThreads;
+    uint64_t i = (uint64_t)blockIdx.x * kPThreads + threadIdx.x;
+    for (; i + 3 * stride < n4; i += 4 * stride) {
+      uint4 a[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) a[u] = v4[i + u * stride];
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        m = max(m, max(max(a[u].x, a[u].y), max(a[u].z, a[u].w)));
+    }
+    for (; i < n4; i += stride) {
+      const uint4 a = v4[i];
+      m = max(m, max(max(a.x, a.y), max(a.z, a.w)));
+    }
+    if (blockIdx.x == 0 && threadIdx.x < (stored & 3)) m = max(m, values[n4 * 4 + threadIdx.x]);
   }
   m = __reduce_max_sync(0xffffffffu, m);
   if ((threadIdx.x & 31) == 0) s_max[threadIdx.x >> 5] = m;
@@ -288,14 +330,14 @@ __global__ void __launch_bounds__(kPThreads) k_parse_finish(const uint32_t* valu
   if (threadIdx.x == 0) {
     uint32_t b = 0;
     for (int w = 0; w < kPThreads / 32; ++w) b = s_max[w] > b ? s_max[w] : b;
-    atomicMax(&ctrl->max_value, b);
+    if (recompute) atomicMax(&ctrl->recomputed_max, b);
     __threadfence();
     const uint32_t done = atomicAdd(&ctrl->done_blocks, 1u);
     if (done == gridDim.x - 1) {
       __threadfence();
       res->values = count;
       res->tokens = ctrl->tokens;
-      res->max_value = atomicAdd(&ctrl->max_value, 0u);
+      res->max_value = recompute ? atomicAdd(&ctrl->recomputed_max, 0u) : ctrl->max_value;
       res->status = count > cap ? WAH_EOVERFLOW : WAH_OK;
       res->reserved = 0;
     }
@@ -321,7 +363,8 @@ int wah_parse_text(const void* d_text, uint64_t bytes, uint32_t* d_values, uint6
                    void* stream) {
   if (!d_result || (reinterpret_cast<uintptr_t>(d_result) & 15)) return WAH_EINVAL;
   if (bytes > 0 && (!d_text || (reinterpret_cast<uintptr_t>(d_text) & 15))) return WAH_EINVAL;
-  if (capacity > 0 && !d_values) return WAH_EINVAL;
+  if (capacity > 0 && (!d_values || (reinterpret_cast<uintptr_t>(d_values) & 15)))
+    return WAH_EINVAL;
   if (!d_workspace || workspace_bytes < wah_parse_workspace_bytes() ||
       (reinterpret_cast<uintptr_t>(d_workspace) & 15))
     return WAH_ENOMEM;
