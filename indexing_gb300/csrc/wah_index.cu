@@ -365,12 +365,32 @@ __global__ void __launch_bounds__(kBuildThreads, 3)
 
     if (!sm.abort) {
       bool overflow = false;
-      for (uint32_t k = tid; k < tw; k += kBuildThreads) {
-        const uint64_t pos = (uint64_t)run_w + k;
-        if (pos < index_cap)
-          out_index[pos] = sm.words[skew(k)];
-        else
-          overflow = true;
+      if ((uint64_t)run_w + tw <= index_cap &&
+          (reinterpret_cast<uintptr_t>(out_index) & 15) == 0) {
+        // words up to the next 16-byte boundary of the index, then groups of
+        // four with one 16-byte store each, then the rest
+        const uint32_t head = ((4u - (run_w & 3u)) & 3u) < tw ? ((4u - (run_w & 3u)) & 3u) : tw;
+        if (tid < head) out_index[run_w + tid] = sm.words[skew(tid)];
+        const uint32_t groups = (tw - head) >> 2;
+        for (uint32_t g = tid; g < groups; g += kBuildThreads) {
+          const uint32_t k = head + 4 * g;
+          uint4 q;
+          q.x = sm.words[skew(k)];
+          q.y = sm.words[skew(k + 1)];
+          q.z = sm.words[skew(k + 2)];
+          q.w = sm.words[skew(k + 3)];
+          *reinterpret_cast<uint4*>(out_index + run_w + k) = q;
+        }
+        const uint32_t tail = head + 4 * groups;
+        if (tid < tw - tail) out_index[run_w + tail + tid] = sm.words[skew(tail + tid)];
+      } else {
+        for (uint32_t k = tid; k < tw; k += kBuildThreads) {
+          const uint64_t pos = (uint64_t)run_w + k;
+          if (pos < index_cap)
+            out_index[pos] = sm.words[skew(k)];
+          else
+            overflow = true;
+        }
       }
       for (uint32_t k = tid; k < tk; k += kBuildThreads) {
         const uint64_t pos = (uint64_t)run_k + k;
