@@ -369,7 +369,7 @@ uint32_t wah_last_launch_count(void);
 /* Tile shape of the radix digit passes: rows per thread (8, 12 or 16;
  * 256 threads per tile), optionally OR WAH_TUNE_MATCH to build the digit
  * peer masks with match.any instead of ballots, or WAH_TUNE_HYBRID to build
- * half of them each way.  Process-wide; set by the
+ * 3/8 of them with match.any and the rest with ballots.  Process-wide; set by the
  * autotuner or the caller before builds are enqueued.  The reference
  * hard-codes its radix shape (src/phases.cpp:445-453). */
 #define WAH_TUNE_MATCH 0x100

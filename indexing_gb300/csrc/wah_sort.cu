@@ -296,8 +296,15 @@ __device__ __forceinline__ void fetch_tile(uint32_t* dst_k, uint32_t* dst_r, uin
   if (rin) bulk_copy_g2s(dst_r, rin + base, bytes, bar);
 }
 
-// PEERS: 0 all items by ballots, 1 all by match.any, 2 the first half by
-// match.any and the second by ballots (the two pipes work in parallel).
+// PEERS: 0 all items by ballots, 1 all by match.any, 2 the first
+// kHybridMatchItems by match.any and the rest by ballots (the two pipes work
+// in parallel).
+#ifndef WAH_HYBRID_MATCH_NUM
+#define WAH_HYBRID_MATCH_NUM 3  // match.any share of the items: NUM / 8 (measured best)
+#endif
+__host__ __device__ constexpr int kHybridMatchItems(int items) {
+  return items * WAH_HYBRID_MATCH_NUM / 8;
+}
 template <int ITEMS, int PEERS, class G>
 __global__ void __launch_bounds__(kSortThreads, 2)
     k_radix_scatter(G g, int pass, const uint32_t* __restrict__ range_start) {
@@ -388,7 +395,7 @@ __global__ void __launch_bounds__(kSortThreads, 2)
     uint32_t rank[ITEMS];
 #pragma unroll
     for (int j = 0; j < ITEMS; ++j) {
-      const bool ballot = PEERS == 0 || (PEERS == 2 && j >= HALF);
+      const bool ballot = PEERS == 0 || (PEERS == 2 && j >= kHybridMatchItems(ITEMS));
       rank[j] = ballot ? digit_peers<true>(digit8(key[j], pass))
                        : digit_peers<false>(digit8(key[j], pass));
     }
