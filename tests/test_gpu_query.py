@@ -209,3 +209,29 @@ def test_query_output_capacity_is_reported(wah):
     assert lib.wah_query(keys.data_ptr(), offsets.data_ptr(), index.data_ptr(), len(keys),
                          len(index), n, 0, 3, 0, 0, 0, None, 0, None, 0, res.data_ptr(),
                          ws.data_ptr(), 16, None) == wah.WAH_ENOMEM
+
+
+def test_largest_column(wah):
+    """The largest column one call accepts, 2^30 - 1 rows (every word
+    position stays within u32): built and decoded back to the column bit for
+    bit on the GPU; 2^30 rows are refused with WAH_ERANGE before any work."""
+    n = (1 << 30) - 1
+    g = torch.Generator(device="cuda")
+    g.manual_seed(30)
+    col = torch.randint(0, 65536, (n,), device="cuda", dtype=torch.int32, generator=g)
+    idx = wah.build_index(col, bound=65535)
+    assert len(idx.keys) == 65536
+    assert n < len(idx.index) < 2 * n
+    d = wah.decode(idx, n, rows=False, column=True, key_rows=True)
+    assert torch.equal(d["column"], col)
+    starts = d["key_rows"].long()
+    assert int(starts[0].item()) == 0 and bool((starts[1:] > starts[:-1]).all())
+    del d, idx, starts
+    torch.cuda.empty_cache()
+    # 2^30 rows through the C ABI: refused before anything is read or written
+    lib = wah._lib.load()
+    counts = torch.zeros(4, dtype=torch.int32, device="cuda")
+    dummy = torch.zeros(4, dtype=torch.int32, device="cuda")
+    p = dummy.data_ptr()
+    rc = lib.wah_build(p, 1 << 30, 65535, p, p, p, counts.data_ptr(), p, 16, None)
+    assert rc == wah.WAH_ERANGE
