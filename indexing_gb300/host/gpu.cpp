@@ -67,7 +67,7 @@ struct merger_state {
   uint32_t bound = 0;
   std::string output;
   std::chrono::steady_clock::time_point start;
-  wahmerge::slice_merger index;
+  wahmerge::slice_merger index{std::min(16u, std::max(1u, std::thread::hardware_concurrency()))};
   std::map<uint64_t, slice_index> pending;  // slices that arrived early
   int status = WAH_OK;
   int* exit_code = nullptr;

@@ -101,6 +101,32 @@ int main() {
             ++failures;
           }
         }
+  // large slices merged by several threads (the parallel path), against the
+  // whole column and against the one-thread merge
+  {
+    const size_t n = 3000000, slice = 31 * 40000;
+    std::vector<uint32_t> v(n);
+    for (size_t i = 0; i < n; ++i) v[i] = next_u32() % 1000;
+    const built whole = oracle_build(v.data(), n);
+    wahmerge::slice_merger par(4), one(1);
+    for (size_t start = 0; start < n; start += slice) {
+      const size_t len = std::min(slice, n - start);
+      const built part = oracle_build(v.data() + start, len);
+      for (wahmerge::slice_merger* m : {&par, &one})
+        m->add(start, len, part.keys.data(), part.offsets.data(),
+               static_cast<uint32_t>(part.keys.size()), part.index.data(),
+               static_cast<uint32_t>(part.index.size()));
+    }
+    built a, b;
+    par.finish(&a.keys, &a.offsets, &a.index);
+    one.finish(&b.keys, &b.offsets, &b.index);
+    ++cases;
+    if (a.keys != whole.keys || a.offsets != whole.offsets || a.index != whole.index ||
+        b.index != whole.index) {
+      std::fprintf(stderr, "mismatch: threaded merge of 3M rows\n");
+      ++failures;
+    }
+  }
   // a slice that does not start on a chunk boundary is refused
   {
     wahmerge::slice_merger m;

@@ -42,7 +42,7 @@ def test_slice_merger_matches_whole_column_index(tmp_path):
     exe = tmp_path / "merge_test"
     subprocess.run(["gcc", "-O2", "-std=c99", "-c", os.path.join(ORACLE_DIR, "wah_oracle.c"),
                     "-o", str(obj)], check=True)
-    subprocess.run(["g++", "-O2", "-std=c++17", "-I" + _lib.HOST_DIR, "-I" + ORACLE_DIR,
+    subprocess.run(["g++", "-O2", "-std=c++17", "-pthread", "-I" + _lib.HOST_DIR, "-I" + ORACLE_DIR,
                     os.path.join(REPO, "tests", "native", "merge_test.cpp"), str(obj),
                     "-o", str(exe)], check=True)
     r = run([str(exe)])
