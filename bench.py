@@ -596,7 +596,7 @@ def main():
     # DRAM bytes per row of each phase's kernels (dram__bytes_read.sum +
     # dram__bytes_write.sum, one ncu capture of a 67,108,864-row uniform
     # 16-bit column with the same tile shape); traffic grows with rows.
-    traffic_per_row = {"histogram": 4.05, "pass0": 15.18, "pass1": 23.30, "build": 23.33}
+    traffic_per_row = {"histogram": 4.05, "pass0": 15.11, "pass1": 23.25, "build": 23.37}
     alg = {"histogram": 4 * n, "plan": 0, "pass0": 12 * n, "pass1": 16 * n, "pass2": 0,
            "pass3": 0, "build": 8 * n + 4 * L + 8 * K}
     per_unit = {"histogram": "4 B/row", "pass0": "12 B/row",
