@@ -162,3 +162,44 @@ def test_text_reading_stops_like_a_stream(cpu_prog, tmp_path):
     data.write_text("1 4294967296 2\n")  # overflow ends the stream too
     r = run([cpu_prog, "-f", str(data)])
     assert "'1' values." in r.stdout
+
+
+def test_generate_workload_distributions(progs):
+    """The benchmark workloads' columns from `generate`: Zipf frequencies
+    follow r^-s, `few` has exactly the requested distinct values, runs have
+    the requested mean length; all seeded and within [from, to]."""
+    g = progs["generate"]
+    n = 400_000
+    z = np.array(run([g, "-a", str(n), "--dist", "zipf", "--zipf-s", "1.1", "--seed", "3"])
+                 .stdout.split(), dtype=np.int64)
+    assert z.size == n and z.min() >= 0 and z.max() <= 65535
+    w = 1.0 / np.arange(1, 65537, dtype=np.float64) ** 1.1
+    p = w / w.sum()
+    for r in (0, 1, 9):  # ranks 1, 2, 10
+        assert abs(np.mean(z == r) - p[r]) < 5 * np.sqrt(p[r] / n) + 1e-4
+    again = run([g, "-a", "1000", "--dist", "zipf", "--seed", "3"]).stdout
+    assert again.split() == [str(x) for x in z[:1000]]
+    f = np.array(run([g, "-a", "50000", "--dist", "few", "--distinct", "16", "-f", "100",
+                      "-t", "65535"]).stdout.split(), dtype=np.int64)
+    assert set(np.unique(f)) == set(range(100, 116))
+    r = np.array(run([g, "-a", str(n), "--dist", "runs", "--run-mean", "500"]).stdout.split(),
+                 dtype=np.int64)
+    runs = 1 + np.count_nonzero(np.diff(r))
+    assert 0.85 * 500 < n / runs < 1.15 * 500
+    assert run([g, "--dist", "nope"]).returncode != 0
+    assert run([g, "--dist", "zipf", "-t", "4294967295"]).returncode != 0
+
+
+def test_generate_serving_trace(progs):
+    lines = run([progs["generate"], "--trace", "5000", "--rate", "200", "--seed", "9"]) \
+        .stdout.splitlines()
+    assert len(lines) == 5000
+    t = np.array([float(x.split()[0]) for x in lines])
+    rows = np.array([int(x.split()[1]) for x in lines])
+    kinds = {x.split()[2] for x in lines}
+    assert (np.diff(t) > 0).all()
+    assert 0.9 / 200 < t[-1] / 5000 < 1.1 / 200
+    assert rows.min() >= 10_000 and rows.max() <= 16_777_216
+    # log-uniform sizes: the median near the geometric mean of the bounds
+    assert 0.7 < np.median(rows) / np.sqrt(10_000 * 16_777_216) < 1.4
+    assert kinds == {"uniform", "zipf", "runs"}
