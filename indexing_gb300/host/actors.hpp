@@ -171,14 +171,18 @@ class actor_system {
   }
 
   // Ends an actor after its current message; pending messages are dropped.
+  // Its behavior (whose handlers hold the actor's context, and through it
+  // the actor itself) is released as soon as no handler of it runs.
   void quit(actor_core* c) {
     std::function<void()> cb;
+    behavior dead;
     {
       std::lock_guard<std::mutex> lk(c->mu);
       if (c->quit) return;
       c->quit = true;
       c->mailbox.clear();
       cb = std::move(c->on_quit);
+      if (!c->scheduled) dead = std::move(c->beh);  // not running nor queued
     }
     if (cb) cb();
     if (alive_.fetch_sub(1) == 1) {
@@ -206,8 +210,10 @@ class actor_system {
       // one message per turn keeps actors fair
       envelope e;
       {
+        behavior dead;
         std::lock_guard<std::mutex> lk(c->mu);
         if (c->mailbox.empty() || c->quit) {
+          if (c->quit) dead = std::move(c->beh);
           c->scheduled = false;
           continue;
         }
@@ -218,12 +224,17 @@ class actor_system {
         // unmatched messages are dropped, as CAF does with unexpected ones
       }
       bool again = false;
+      behavior dead;  // a quit actor's behavior, released outside the lock
       {
         std::lock_guard<std::mutex> lk(c->mu);
-        if (!c->mailbox.empty() && !c->quit)
-          again = true;
-        else
+        if (c->quit) {
+          dead = std::move(c->beh);
           c->scheduled = false;
+        } else if (!c->mailbox.empty()) {
+          again = true;
+        } else {
+          c->scheduled = false;
+        }
       }
       if (again) {
         std::lock_guard<std::mutex> lk(mu_);
