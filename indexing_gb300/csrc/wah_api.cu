@@ -5,6 +5,7 @@
 // src/phases.cpp:713-1088 (spawned kernel actors + mem_ref buffers) and the
 // per-batch worker of src/gpu.cpp:356-367.
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <new>
 
@@ -13,8 +14,9 @@
 namespace wah {
 
 thread_local uint32_t g_last_launches = 0;
-int g_sort_items = 16;  // radix tile rows per thread (wah_set_tuning)
-int g_sort_peers = 0;   // peer-mask mode (wah_set_tuning)
+// Tile shape of the digit passes (wah_set_tuning): rows per thread | peer
+// mode flags, one atomic word so concurrent builds read a consistent pair.
+std::atomic<int> g_tuning{16};
 
 uint32_t* last_launches_slot() { return &g_last_launches; }
 
@@ -25,13 +27,16 @@ int passes_for_bound(uint32_t bound) {
 }
 
 int sm_count_current() {
-  static int cached[64] = {0};
+  static std::atomic<int> cached[64];
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return 0;
-  if (dev < 64 && cached[dev]) return cached[dev];
+  if (dev >= 0 && dev < 64) {
+    const int c = cached[dev].load(std::memory_order_relaxed);
+    if (c) return c;
+  }
   int sms = 0;
   if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
-  if (dev < 64) cached[dev] = sms;
+  if (dev >= 0 && dev < 64) cached[dev].store(sms, std::memory_order_relaxed);
   return sms;
 }
 
@@ -46,8 +51,9 @@ int cuda_status(cudaError_t e) {
 
 LaunchOpts launch_opts(int max_passes, cudaEvent_t* events) {
   LaunchOpts o;
-  o.sort_items = g_sort_items;
-  o.sort_peers = g_sort_peers;
+  const int t = g_tuning.load(std::memory_order_relaxed);
+  o.sort_items = t & 0xff;
+  o.sort_peers = (t & WAH_TUNE_MATCH) ? 1 : (t & WAH_TUNE_HYBRID) ? 2 : 0;
   o.max_passes = max_passes;
   o.sm_count = sm_count_current();
   o.events = events;
@@ -147,15 +153,12 @@ int wah_set_tuning(int sort_items) {
   const int items = sort_items & 0xff;
   if (items != 8 && items != 12 && items != 16) return WAH_EINVAL;
   if ((sort_items & WAH_TUNE_MATCH) && (sort_items & WAH_TUNE_HYBRID)) return WAH_EINVAL;
-  g_sort_items = items;
-  g_sort_peers = (sort_items & WAH_TUNE_MATCH) ? 1 : (sort_items & WAH_TUNE_HYBRID) ? 2 : 0;
+  if (sort_items & ~(0xff | WAH_TUNE_MATCH | WAH_TUNE_HYBRID)) return WAH_EINVAL;
+  g_tuning.store(sort_items, std::memory_order_relaxed);
   return WAH_OK;
 }
 
-int wah_get_tuning(void) {
-  return g_sort_items | (g_sort_peers == 1 ? WAH_TUNE_MATCH : 0) |
-         (g_sort_peers == 2 ? WAH_TUNE_HYBRID : 0);
-}
+int wah_get_tuning(void) { return g_tuning.load(std::memory_order_relaxed); }
 
 static int build_impl(const uint32_t* d_values, uint64_t n, uint32_t bound, uint32_t* d_keys,
                       uint32_t* d_offsets, uint32_t* d_index, wah_counts* d_counts,
