@@ -47,7 +47,10 @@ REPO = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, REPO)
 
 METRIC = "rows/s & HBM GB/s at 256M u32; batched rows/s + p50/p99 vs plain, bit-exact"
-PHASES = ["histogram", "plan", "pass0", "pass1", "pass2", "pass3", "build"]
+# wah_build_timed spans: phases, then single kernels inside them
+PHASES = ["histogram", "plan", "pass0", "pass1", "pass2", "pass3", "build",
+          "scatter0", "scatter1", "scatter2", "scatter3", "emit"]
+KERNELS = ["histogram", "scatter0", "scatter1", "scatter2", "scatter3", "emit"]
 
 
 def parse():
@@ -590,22 +593,29 @@ def main():
     max_ms, value = replica_throughput(elapsed_ms, n, args.steps, dist, dev)
     ms_per_step = max_ms / args.steps
 
-    # Algorithmic bytes (per build; integer keys <= 16 bits -> 2 digit passes):
-    #   histogram 4n, pass0 12n (read key, write key+rid), pass1 16n,
-    #   build 8n + 4L + 8K (read sorted key+rid, write words, keys, offsets)
-    # DRAM bytes per row of each phase's kernels (dram__bytes_read.sum +
+    # Algorithmic bytes per build: histogram 4n; digit pass 0 12n (read key,
+    # write key + rid), later passes 16n; build 8n + 4L + 8K (read sorted
+    # key + rid, write words, keys, offsets).  A phase (count + scan +
+    # kernel) and its main kernel are credited the same bytes; the roofline
+    # is taken on the longest single kernel.
+    passes = max(1, -(-(card - 1).bit_length() // 8))
+    alg = {"histogram": 4 * n, "plan": 0, "build": 8 * n + 4 * L + 8 * K}
+    alg["emit"] = alg["build"]
+    for p in range(4):
+        a = (12 * n if p == 0 else 16 * n) if p < passes else 0
+        alg[f"pass{p}"] = a
+        alg[f"scatter{p}"] = a
+    # DRAM bytes per row of each kernel (dram__bytes_read.sum +
     # dram__bytes_write.sum, one ncu capture of a 67,108,864-row uniform
     # 16-bit column with the same tile shape); traffic grows with rows.
-    traffic_per_row = {"histogram": 4.05, "pass0": 15.11, "pass1": 23.25, "build": 23.37}
-    alg = {"histogram": 4 * n, "plan": 0, "pass0": 12 * n, "pass1": 16 * n, "pass2": 0,
-           "pass3": 0, "build": 8 * n + 4 * L + 8 * K}
-    per_unit = {"histogram": "4 B/row", "pass0": "12 B/row",
-                "pass1": "16 B/row (range count + scan + scatter timed together)",
-                "build": "8 B/row + 4 B/word + 8 B/key"}
-    dom = max(PHASES, key=lambda p: phase_ms[p])
+    traffic_per_row = {"histogram": 4.05, "scatter0": 15.11, "scatter1": 19.20, "emit": 15.32}
+    per_unit = {"histogram": "4 B/row", "scatter0": "12 B/row (key in, key + rid out)",
+                "scatter1": "16 B/row (key + rid in and out)",
+                "emit": "8 B/row + 4 B/word + 8 B/key"}
+    dom = max(KERNELS, key=lambda p: phase_ms[p])
     peak, peak_kind = load_peaks()
     ach = alg[dom] / (phase_ms[dom] / 1e3) / 1e9 if phase_ms[dom] > 0 else 0.0
-    total_alg = sum(alg.values())
+    total_alg = sum(alg[p] for p in ("histogram", "pass0", "pass1", "pass2", "pass3", "build"))
     for p in PHASES:
         if rank == 0:
             gbs = alg[p] / (phase_ms[p] / 1e3) / 1e9 if phase_ms[p] > 0 and alg[p] else 0
@@ -679,7 +689,11 @@ def main():
             "autotune": tuned,
             "hbm_gbs_pipeline": total_alg / (ms_per_step / 1e3) / 1e9,
             "phase_us": {p: round(phase_ms[p] * 1e3, 1) for p in PHASES},
-            "roofline": {"bound": "hbm", "kernel": dom, "per_unit": per_unit.get(dom),
+            "roofline": {"bound": "hbm", "kernel": {"scatter0": "k_radix_scatter (pass 0)",
+                                                    "scatter1": "k_radix_scatter (pass 1)",
+                                                    "emit": "k_build_emit",
+                                                    "histogram": "k_digit_histogram"}.get(dom, dom),
+                         "per_unit": per_unit.get(dom),
                          "achieved": ach, "peak": peak, "unit": "GB/s",
                          "frac": ach / peak, "peak_kind": peak_kind,
                          "traffic": (traffic_per_row[dom] * n

@@ -396,11 +396,14 @@ int wah_autotune(uint64_t n, uint32_t bound, const char* cache_path, int* chosen
  * CUDA events on the build's own stream instead of host clocks around
  * synchronisations.  wah_build_timed is wah_build plus event records around
  * each kernel: events[2p] before and events[2p+1] after phase p, for the
- * WAH_TIMED_PHASES phases histogram, plan, digit passes 0..3, index build
- * (a pass that is not launched gets an empty span).  Events come from
- * wah_events_create; durations from wah_events_elapsed after a sync.
+ * WAH_TIMED_PHASES phases: 0 histogram, 1 plan, 2..5 digit passes 0..3
+ * (count, scan and scatter), 6 index build (count, scan, emit), and single
+ * kernels inside them: 7..10 the scatter kernel of passes 0..3, 11 the
+ * build's emit kernel (a pass that is not launched gets empty spans).
+ * Events come from wah_events_create; durations from wah_events_elapsed
+ * after a sync.
  */
-#define WAH_TIMED_PHASES 7
+#define WAH_TIMED_PHASES 12
 int wah_events_create(uint32_t count, void** events);
 void wah_events_destroy(uint32_t count, void** events);
 int wah_events_elapsed(void* start, void* end, float* ms);

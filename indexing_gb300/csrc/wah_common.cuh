@@ -249,12 +249,16 @@ __device__ __forceinline__ uint64_t block_exclusive_scan64(uint64_t x, uint64_t*
 
 #endif  // __CUDACC__
 
-// Timed phases (wah_build_timed): histogram, plan, four digit passes, build.
+// Timed phases (wah_build_timed): histogram, plan, four digit passes, build;
+// then spans of single kernels inside them: each pass's scatter kernel and
+// the build's emit kernel.
 constexpr int kPhaseHist = 0;
 constexpr int kPhasePlan = 1;
 constexpr int kPhasePass0 = 2;
 constexpr int kPhaseBuild = 6;
-constexpr int kPhases = 7;
+constexpr int kPhaseScatter0 = 7;
+constexpr int kPhaseEmit = 11;
+constexpr int kPhases = 12;
 
 inline void record_phase(cudaEvent_t* ev, int phase, bool end, cudaStream_t s) {
   if (ev) cudaEventRecord(ev[2 * phase + (end ? 1 : 0)], s);

@@ -424,7 +424,9 @@ cudaError_t launch_build_t(const G& g, uint32_t ncols, uint32_t ranges, const Ra
   record_phase(o.events, kPhaseBuild, false, s);
   k_build_count<G><<<ranges * kCountCtasPerRange, kHistThreads, 0, s>>>(g, ra.counts);
   k_build_scan<G><<<ncols, kBuildScanThreads, 0, s>>>(g, ra.counts, ra.first);
+  record_phase(o.events, kPhaseEmit, false, s);
   k_build_emit<G><<<ranges, kBuildThreads, smem, s>>>(g, ra.first);
+  record_phase(o.events, kPhaseEmit, true, s);
   record_phase(o.events, kPhaseBuild, true, s);
   *launches += 3;
   return cudaGetLastError();

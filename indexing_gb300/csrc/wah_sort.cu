@@ -536,9 +536,11 @@ cudaError_t launch_sort_t(const G& g, uint32_t ncols, uint32_t ranges, const Ran
   err = cudaGetLastError();
   if (err != cudaSuccess) return err;
   for (int p = 0; p < kDigits; ++p) {
-    if (p >= o.max_passes) {  // not launched: empty span keeps every event valid
+    if (p >= o.max_passes) {  // not launched: empty spans keep every event valid
       record_phase(o.events, kPhasePass0 + p, false, s);
       record_phase(o.events, kPhasePass0 + p, true, s);
+      record_phase(o.events, kPhaseScatter0 + p, false, s);
+      record_phase(o.events, kPhaseScatter0 + p, true, s);
       continue;
     }
     uint32_t* rh = ra.hist + (size_t)p * ra.max_ranges * kRadix;
@@ -549,8 +551,10 @@ cudaError_t launch_sort_t(const G& g, uint32_t ncols, uint32_t ranges, const Ran
     }
     k_range_scan<G><<<ncols, kRadix, 0, s>>>(g, p, rh, ra.start);
     ++*launches;
+    record_phase(o.events, kPhaseScatter0 + p, false, s);
     v.fn<<<ranges, kSortThreads, v.smem, s>>>(g, p, ra.start);
     ++*launches;
+    record_phase(o.events, kPhaseScatter0 + p, true, s);
     record_phase(o.events, kPhasePass0 + p, true, s);
     err = cudaGetLastError();
     if (err != cudaSuccess) return err;
