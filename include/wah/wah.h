@@ -362,6 +362,28 @@ int wah_noop_graph_create(uint32_t count, wah_noop_graph** out);
 int wah_noop_graph_launch(wah_noop_graph* graph, void* stream);
 void wah_noop_graph_destroy(wah_noop_graph* graph);
 
+/*
+ * Incremental append on the device.  A = the index (keys, offsets, index) of
+ * rows [0, rows_a) of a column, B = the index of the next rows [rows_a,
+ * rows_a + n) built alone (rows_a a multiple of 31).  wah_append writes the
+ * index of all rows_a + n rows -- word for word what one build of the whole
+ * column gives -- to out_* (keys_cap >= keycnt_a + keycnt_b, index_cap >=
+ * index_len_a + index_len_b + keycnt_b).  The reference's `gpu` merger
+ * appends slice bitmaps without re-basing their leading fills
+ * (src/gpu.cpp:103-165); here B's leading fill per key becomes the zero
+ * chunks since the key's last row in A.  d_counts receives K, L and a
+ * status (WAH_ECORRUPT when A has rows at or past rows_a).  All pointers are
+ * device memory; workspace wah_append_workspace_bytes(keycnt_a, keycnt_b).
+ */
+size_t wah_append_workspace_bytes(uint32_t keycnt_a, uint32_t keycnt_b);
+int wah_append(const uint32_t* a_keys, const uint32_t* a_offsets,
+               const uint32_t* a_index, uint32_t keycnt_a, uint32_t index_len_a,
+               uint64_t rows_a, const uint32_t* b_keys, const uint32_t* b_offsets,
+               const uint32_t* b_index, uint32_t keycnt_b, uint32_t index_len_b,
+               uint32_t* out_keys, uint32_t* out_offsets, uint32_t* out_index,
+               uint64_t keys_cap, uint64_t index_cap, wah_counts* d_counts,
+               void* d_workspace, size_t workspace_bytes, void* stream);
+
 /* Number of kernels the last wah_build/wah_ctx_build_host on this thread
  * enqueued (launch accounting for benchmarks). */
 uint32_t wah_last_launch_count(void);

@@ -15,6 +15,8 @@ Python face of the C ABI in ``include/wah/wah.h`` (library
                              (src/cpu.cpp:47-74)
 * :func:`decode`             every key's rows on the GPU (row ids, the
                              sorted column, the column itself)
+* :func:`append`             the index of more rows appended to an index on
+                             the GPU (incremental builds)
 * :func:`parse_text`         the reference's text data files (one value per
                              line) parsed on the GPU into a column
 * :func:`query`              rows of a key / value range, or of two ranges
@@ -37,7 +39,7 @@ from ._lib import wah_counts
 
 __all__ = ["WahError", "WahIndex", "build_index", "sort_rids_by_value", "build_sorted",
            "HostContext", "Pipeline", "Batch", "Server", "decoded_bitmap", "workspace_bytes", "output_caps",
-           "MAX_ROWS", "last_launch_count", "autotune", "decode", "query", "parse_text", "QUERY_KEYS", "QUERY_OR",
+           "MAX_ROWS", "last_launch_count", "autotune", "decode", "query", "parse_text", "append", "QUERY_KEYS", "QUERY_OR",
            "QUERY_AND", "QUERY_ANDNOT"]
 
 MAX_ROWS = 1 << 30
@@ -138,7 +140,10 @@ def _as_device_u32(values, device):
         raise TypeError("values must be a 32-bit integer tensor")
     if t.dtype == torch.uint32:
         t = t.view(torch.int32)
-    return t.to(device).contiguous()
+    t = t.to(device).contiguous()
+    if t.data_ptr() % 16:  # a view into a larger tensor: the kernels want 16-byte alignment
+        t = t.clone()
+    return t
 
 
 class _Buffers:
@@ -279,6 +284,35 @@ def parse_text(data, capacity: int | None = None, stream=None, device="cuda"):
         raise WahError(int(r.status), "wah_parse_text (device)")
     info = {"values": int(r.values), "tokens": int(r.tokens), "max_value": int(r.max_value)}
     return out[:int(r.values)], info
+
+
+def append(a: WahIndex, rows_a: int, b: WahIndex, stream=None) -> WahIndex:
+    """The index of rows_a + n rows from ``a`` (rows [0, rows_a); rows_a a
+    multiple of 31) and ``b`` (the next n rows, built alone), on the GPU;
+    word for word the index one build of all rows gives.  ``merged`` of the
+    result is 0 (not tracked)."""
+    lib = _lib.load()
+    torch = _torch()
+    ak, ao, ai, dev = _index_tensors(a)
+    bk, bo, bi, _ = _index_tensors(b)
+    ka, la, kb, lb = len(a.keys), len(a.index), len(b.keys), len(b.index)
+    kc, ic = ka + kb, la + lb + kb
+    out_k = torch.empty(max(kc, 1), dtype=torch.int32, device=dev)
+    out_o = torch.empty(max(kc, 1), dtype=torch.int32, device=dev)
+    out_i = torch.empty(max(ic, 1), dtype=torch.int32, device=dev)
+    counts = torch.zeros(4, dtype=torch.int32, device=dev)
+    wsb = int(lib.wah_append_workspace_bytes(ka, kb))
+    ws = torch.empty(wsb, dtype=torch.uint8, device=dev)
+    rc = lib.wah_append(ak.data_ptr(), ao.data_ptr(), ai.data_ptr(), ka, la, rows_a,
+                        bk.data_ptr(), bo.data_ptr(), bi.data_ptr(), kb, lb, out_k.data_ptr(),
+                        out_o.data_ptr(), out_i.data_ptr(), max(kc, 1), max(ic, 1),
+                        counts.data_ptr(), ws.data_ptr(), wsb, _stream_handle(stream))
+    _check(rc, "wah_append")
+    c = counts.cpu().numpy().view(np.uint32)
+    if c[3] != WAH_OK:
+        raise WahError(int(c[3]), "wah_append (device)")
+    K, L = int(c[0]), int(c[1])
+    return WahIndex(out_k[:K], out_o[:K], out_i[:L], 0)
 
 
 def _term(t):

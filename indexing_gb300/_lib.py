@@ -21,7 +21,7 @@ LIB_PATH = os.path.join(PKG_DIR, "libwah_gb300.so")
 
 CUDA_SOURCES = ["wah_sort.cu", "wah_index.cu", "wah_api.cu", "wah_batch.cu", "wah_pipe.cu",
                 "wah_serve.cu", "wah_noalloc.cu", "wah_query.cu", "wah_ingest.cu",
-                "wah_tune.cu"]
+                "wah_tune.cu", "wah_append.cu"]
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo",
               "-std=c++17", "-Xcompiler", "-fPIC", "-I" + INCLUDE, "-I" + CSRC]
 
@@ -182,6 +182,9 @@ SIGNATURES = {
     "wah_noop_graph_create": ([_u32, ctypes.POINTER(_vp)], ctypes.c_int),
     "wah_noop_graph_launch": ([_vp, _vp], ctypes.c_int),
     "wah_noop_graph_destroy": ([_vp], None),
+    "wah_append_workspace_bytes": ([_u32, _u32], ctypes.c_size_t),
+    "wah_append": ([_vp, _vp, _vp, _u32, _u32, _u64, _vp, _vp, _vp, _u32, _u32, _vp, _vp, _vp,
+                    _u64, _u64, _vp, _vp, ctypes.c_size_t, _vp], ctypes.c_int),
     "wah_last_launch_count": ([], _u32),
     "wah_device_count": ([], ctypes.c_int),
     "wah_device_name": ([ctypes.c_int, ctypes.c_char_p, ctypes.c_size_t], ctypes.c_int),
