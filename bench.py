@@ -23,6 +23,9 @@ SHOW_TIME_CONSUMPTION output, src/phases.cpp:714-1127) go to stderr.
               one-key / 1,000-key range queries
   ingest      the column as a one-value-per-line text file parsed on the
               device (resident text, and from pinned host memory)
+  append      the index of the first ~3/4 of the column and the index of the
+              rest appended on the device (wah_append), checked word for word
+              against the whole-column build
 
 --impl reference times the reference CPU implementation (the oracle port:
 the reference's own sources are not on the GPU machine) on all host threads.
@@ -72,6 +75,7 @@ def parse():
     ap.add_argument("--tune-cache", default=None, help="autotuner cache file")
     ap.add_argument("--no-ingest", action="store_true")
     ap.add_argument("--no-decode", action="store_true")
+    ap.add_argument("--no-append", action="store_true")
     ap.add_argument("--serve-requests", type=int, default=20000)
     ap.add_argument("--serve-budget-gb", type=int, default=64)
     ap.add_argument("--pipe-depth", type=int, default=3,
@@ -387,6 +391,58 @@ def bench_decode(args, lib, torch, dev, stream, bufs, n, K, L):
     return out
 
 
+def bench_append(args, lib, wah, torch, dev, stream, d_values, n, bound, bufs, K, L):
+    """Incremental build: the index of the column's first R rows (R about
+    3/4 of n, a multiple of 124 so both slices start 16-byte aligned) and the
+    index of the remaining n - R rows, appended on the device (wah_append);
+    the result is checked word for word against the whole-column build."""
+    sh = stream.cuda_stream
+    R = (3 * n // 4) // 124 * 124
+    parts = []
+    for start, rows in ((0, R), (R, n - R)):
+        b = wah._Buffers(rows, bound, dev)
+        rc = lib.wah_build(d_values.data_ptr() + 4 * start, rows, bound, b.keys.data_ptr(),
+                           b.offsets.data_ptr(), b.index.data_ptr(), b.counts.data_ptr(),
+                           b.ws.data_ptr(), b.ws_bytes, sh)
+        assert rc == 0
+        c = b.counts.cpu().numpy().view(np.uint32)
+        assert c[3] == 0
+        parts.append((b, int(c[0]), int(c[1])))
+    (a, ka, la), (b, kb, lb) = parts
+    kc, ic = ka + kb, la + lb + kb
+    out_k = torch.empty(kc, dtype=torch.int32, device=dev)
+    out_o = torch.empty(kc, dtype=torch.int32, device=dev)
+    out_i = torch.empty(ic, dtype=torch.int32, device=dev)
+    cnt = torch.zeros(4, dtype=torch.int32, device=dev)
+    wsb = int(lib.wah_append_workspace_bytes(ka, kb))
+    ws = torch.empty(max(wsb, 1), dtype=torch.uint8, device=dev)
+
+    def app():
+        rc = lib.wah_append(a.keys.data_ptr(), a.offsets.data_ptr(), a.index.data_ptr(), ka, la, R,
+                            b.keys.data_ptr(), b.offsets.data_ptr(), b.index.data_ptr(), kb, lb,
+                            out_k.data_ptr(), out_o.data_ptr(), out_i.data_ptr(), kc, ic,
+                            cnt.data_ptr(), ws.data_ptr(), wsb, sh)
+        assert rc == 0
+    app()
+    ms = time_events(app, max(3, args.steps // 5), torch, stream)
+    c = cnt.cpu().numpy().view(np.uint32)
+    assert c[3] == 0
+    Ko, Lo = int(c[0]), int(c[1])
+    exact = (Ko == K and Lo == L and torch.equal(out_k[:K], bufs.keys[:K])
+             and torch.equal(out_o[:K], bufs.offsets[:K]) and torch.equal(out_i[:L], bufs.index[:L]))
+    # algorithmic bytes: A's words walked once for every key's end chunk,
+    # A's and B's words read and the merged words written, keys and offsets
+    # of A and B read and of the result written
+    alg = 4 * la + 4 * (la + lb) + 4 * Lo + 8 * (ka + kb) + 8 * Ko
+    out = {"rows_a": R, "rows_b": n - R, "words_a": la, "words_b": lb, "words_out": Lo,
+           "ms": ms, "appended_rows_per_s": (n - R) / (ms / 1e3),
+           "alg_bytes": alg, "hbm_gbs": alg / (ms / 1e3) / 1e9,
+           "equals_whole_build": bool(exact)}
+    del a, b, parts, out_k, out_o, out_i, ws
+    torch.cuda.empty_cache()
+    return out
+
+
 def bench_serving(args, wah, torch, dev):
     """C5: Poisson arrivals of index-build requests (one pinned host column
     each), rows log-uniform in [10,000, 16,777,216], values uniform [0,65535],
@@ -622,6 +678,8 @@ def main():
             print(f"{p}:\t{phase_ms[p] * 1e3:.0f} us\t{gbs:.0f} GB/s", file=sys.stderr)
 
     decode = None if args.no_decode else bench_decode(args, lib, torch, dev, stream, bufs, n, K, L)
+    append = (None if args.no_append else
+              bench_append(args, lib, wah, torch, dev, stream, d_values, n, bound, bufs, K, L))
     ingest = None if args.no_ingest else bench_ingest(args, lib, torch, dev, stream, d_values, n)
 
     # End to end: host values in, host index out, through the public
@@ -706,6 +764,7 @@ def main():
             "batched": batched,
             "serving": serving,
             "decode": decode,
+            "append": append,
             "ingest": ingest,
             "cpu_baseline": cpu,
         }
