@@ -518,6 +518,35 @@ def cpu_oracle_rate(values: np.ndarray, sample: int, threads: int, repeats: int)
     return threads * sample * repeats / dt, dt
 
 
+def host_cpu():
+    """nproc and the CPU model of this host (for the CPU baselines)."""
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                model = line.split(":", 1)[1].strip()
+                break
+    except Exception:
+        pass
+    if model is None:
+        import platform
+        model = platform.processor() or platform.machine()
+    return {"nproc": os.cpu_count(), "cpu_model": model}
+
+
+def cpu_bubble_time(values: np.ndarray, n: int):
+    """The reference `cpu` program as written sorts by bubble sort
+    (src/cpu.cpp:180-197): the oracle's bubble-sort build of n rows, 1 thread,
+    seconds (timed only at small n; it grows as n^2)."""
+    from oracle import oracle as O
+    O._load()
+    v = np.ascontiguousarray(values[:n])
+    t0 = time.perf_counter()
+    O.build(v, sort_mode=O.SORT_BUBBLE)
+    return time.perf_counter() - t0
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -546,7 +575,8 @@ def run_reference(args):
                                f"{args.seed}", "rows": n, "bound": card - 1},
         "cpu_baseline": {"value": rate, "unit": "rows/s", "cores": threads, "kind": "port",
                          "sample": f"{threads} threads x one oracle build each of {sample} "
-                                   f"rows (disjoint slices of the seeded column) per step"},
+                                   f"rows (disjoint slices of the seeded column) per step",
+                         "host": host_cpu()},
         "e2e": {"value": rate, "unit": "rows/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -727,9 +757,16 @@ def main():
         reps = max(1, min(5, int(10.0 / max(dt, 1e-3))))
         if reps > 1:
             rate, dt = cpu_oracle_rate(values_np, sample, 1, reps)
+        nb = min(16384, n)
+        tb = cpu_bubble_time(values_np, nb)
         cpu = {"value": rate, "unit": "rows/s", "cores": 1, "kind": "port",
                "sample": f"{reps} oracle build(s) of the first {sample} rows of the same "
-                         f"column, 1 thread ({dt:.1f} s)"}
+                         f"column, 1 thread ({dt:.1f} s)",
+               "host": host_cpu(),
+               "bubble_sort_cpu": {"rows": nb, "seconds": tb,
+                                   "extrapolated_seconds_at_n": tb * (n / nb) ** 2,
+                                   "note": "the reference cpu program as written (O(n^2) "
+                                           "bubble sort), 1 thread; n^2 extrapolation"}}
 
     if rank == 0:
         cl = clocks.summary()
@@ -746,6 +783,17 @@ def main():
             "sort_items": int(lib.wah_get_tuning()),
             "autotune": tuned,
             "hbm_gbs_pipeline": total_alg / (ms_per_step / 1e3) / 1e9,
+            # whole-column figure on the scope table's formula (P = 2 digit
+            # passes; the reference's k-sized intermediates included), and the
+            # compulsory I/O (values in, index words, keys and offsets out)
+            "column_roofline": {
+                "formula": "40n + 24k + 4L + 8K",
+                "alg_bytes": 40 * n + 24 * k + 4 * L + 8 * K,
+                "achieved": (40 * n + 24 * k + 4 * L + 8 * K) / (ms_per_step / 1e3) / 1e9,
+                "peak": peak, "unit": "GB/s",
+                "frac": (40 * n + 24 * k + 4 * L + 8 * K) / (ms_per_step / 1e3) / 1e9 / peak,
+                "compulsory_io_bytes": 4 * n + 4 * L + 8 * K,
+                "compulsory_io_gbs": (4 * n + 4 * L + 8 * K) / (ms_per_step / 1e3) / 1e9},
             "phase_us": {p: round(phase_ms[p] * 1e3, 1) for p in PHASES},
             "roofline": {"bound": "hbm", "kernel": {"scatter0": "k_radix_scatter (pass 0)",
                                                     "scatter1": "k_radix_scatter (pass 1)",
