@@ -28,15 +28,82 @@
 namespace wah {
 namespace {
 
-// Walk action: the end chunk of every key.
-struct KeyEndAct {
-  uint32_t* ends;
-  static constexpr bool kNeedsValue = false;
-  static constexpr bool kWantsEnds = true;
-  __device__ __forceinline__ void head(uint32_t, uint32_t) const {}
-  __device__ __forceinline__ void literal(uint32_t, uint32_t, uint32_t, uint32_t) const {}
-  __device__ __forceinline__ void key_end(uint32_t key, uint32_t chunk) const { ends[key] = chunk; }
-};
+// End chunk of every A key: the chunks its words cover (a literal one, a
+// fill its count), summed over the key's words.  Grid-stride tiles of
+// 256 x 16 words; thread t sums words t*16 .. t*16+15 of the tile, finding
+// the key of its first word by binary search over the keys the tile touches.
+// A thread adds each finished key's share with an atomic; a warp whose lanes
+// all end in one key adds their shares with one atomic.  Sums are 64-bit so a
+// corrupt A (fills past row R) cannot wrap back into range.
+constexpr uint32_t kEndItems = 16;
+constexpr uint32_t kEndTile = 256 * kEndItems;
+
+// Last key whose first word is <= i, searched in [lo, hi] (offsets[lo] <= i).
+__device__ __forceinline__ uint32_t key_of_word(const uint32_t* offsets, uint32_t lo, uint32_t hi,
+                                                uint32_t i) {
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi + 1) >> 1;
+    if (offsets[mid] <= i) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+// Tile word i lives at i + i/32 in shared memory: the coalesced loads
+// (consecutive i per warp) and the per-thread reads (i = 16 t + j) both
+// spread over all 32 banks.
+__device__ __forceinline__ uint32_t end_skew(uint32_t i) { return i + (i >> 5); }
+
+__global__ void __launch_bounds__(256) k_key_ends(const uint32_t* __restrict__ offsets,
+                                                  const uint32_t* __restrict__ index,
+                                                  uint32_t ka, uint32_t la,
+                                                  unsigned long long* __restrict__ ends) {
+  __shared__ uint32_t s_w[kEndTile + kEndTile / 32];
+  __shared__ uint32_t s_span[2];
+  const uint32_t ntiles = (uint32_t)ceil_div(la, kEndTile);
+  const uint32_t lane = threadIdx.x & 31;
+  for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const uint32_t t0 = t * kEndTile;
+    const uint32_t t1 = la - t0 < kEndTile ? la : t0 + kEndTile;
+    if (threadIdx.x == 0) {
+      s_span[0] = key_of_word(offsets, 0, ka - 1, t0);
+      s_span[1] = key_of_word(offsets, 0, ka - 1, t1 - 1);
+    }
+#pragma unroll
+    for (uint32_t j = 0; j < kEndItems; ++j) {
+      const uint32_t i = j * 256 + threadIdx.x;
+      s_w[end_skew(i)] = t0 + i < t1 ? index[t0 + i] : 0u;
+    }
+    __syncthreads();
+    const uint32_t k_lo = s_span[0], k_hi = s_span[1];
+    const uint32_t l0 = threadIdx.x * kEndItems;  // this thread's first tile word
+    uint32_t key = kNone;
+    unsigned long long acc = 0;
+    if (t0 + l0 < t1) {
+      key = key_of_word(offsets, k_lo, k_hi, t0 + l0);
+      uint32_t next = key + 1 < ka ? offsets[key + 1] : la;
+      const uint32_t l1 = t1 - t0 - l0 < kEndItems ? t1 - t0 : l0 + kEndItems;
+      for (uint32_t l = l0; l < l1; ++l) {
+        while (t0 + l >= next) {  // the key ended before this word (every key has a word)
+          atomicAdd(&ends[key], acc);
+          acc = 0;
+          ++key;
+          next = key + 1 < ka ? offsets[key + 1] : la;
+        }
+        acc += chunk_advance(s_w[end_skew(l)]);
+      }
+    }
+    const uint32_t key0 = __shfl_sync(0xffffffffu, key, 0);
+    if (__all_sync(0xffffffffu, key == key0 || key == kNone)) {
+#pragma unroll
+      for (int d = 16; d > 0; d >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, d);
+      if (lane == 0 && key0 != kNone) atomicAdd(&ends[key0], acc);
+    } else if (key != kNone) {
+      atomicAdd(&ends[key], acc);
+    }
+    __syncthreads();  // s_w and s_span are rewritten by the next tile
+  }
+}
 
 // ---------------------------------------------------------------------------
 // Exclusive scan of n u32 values (look-back free: per-range sums, one CTA
@@ -171,10 +238,10 @@ struct KeyParts {
   bool has_b;
 };
 
-__device__ __forceinline__ KeyParts key_parts(const AppendIn& in, const uint32_t* ends,
+__device__ __forceinline__ KeyParts key_parts(const AppendIn& in, const unsigned long long* ends,
                                               uint32_t ia, uint32_t jb, uint32_t* status) {
   KeyParts k = {0, 0, 0, 0, 0, false};
-  uint32_t end_a = 0;
+  uint64_t end_a = 0;
   if (ia != kNone) {
     k.a_begin = in.a_offsets[ia];
     k.a_len = (ia + 1 < in.ka ? in.a_offsets[ia + 1] : in.la) - k.a_begin;
@@ -205,7 +272,7 @@ __device__ __forceinline__ KeyParts key_parts(const AppendIn& in, const uint32_t
 // Words per output key; pieces of the copy per key.
 constexpr uint32_t kPiece = 4096;
 
-__global__ void k_key_words(AppendIn in, const uint32_t* ends, const uint32_t* src_a,
+__global__ void k_key_words(AppendIn in, const unsigned long long* ends, const uint32_t* src_a,
                             const uint32_t* src_b, const uint32_t* out_count, uint32_t* words,
                             uint32_t* pieces, uint32_t* status) {
   const uint32_t K = *out_count;
@@ -216,30 +283,38 @@ __global__ void k_key_words(AppendIn in, const uint32_t* ends, const uint32_t* s
   }
 }
 
-// Every piece: find its key (the last key whose first piece is <= it), copy
-// up to kPiece words of A's or B's part; the first thread of the key's first
-// piece writes the gap word.
+// Every piece: copy up to kPiece words of one key's A or B part.  Each CTA
+// takes a contiguous share of the pieces: one binary search finds the key
+// of its first piece (the last key whose first piece is <= it), later pieces
+// step forward; each thread loads its 16 words of a piece before storing any.
+constexpr uint32_t kPieceItems = kPiece / kAThreads;
+static_assert(kPiece % kAThreads == 0, "whole items per thread");
+
 __global__ void __launch_bounds__(kAThreads) k_copy_pieces(
-    AppendIn in, const uint32_t* ends, const uint32_t* src_a, const uint32_t* src_b,
+    AppendIn in, const unsigned long long* ends, const uint32_t* src_a, const uint32_t* src_b,
     const uint32_t* out_count, const uint32_t* piece_base, const uint32_t* total_pieces,
     const uint32_t* out_offsets, uint32_t* out_index, uint32_t* status) {
   __shared__ uint32_t s_key;
   const uint32_t K = *out_count;
   const uint32_t T = *total_pieces;
-  for (uint32_t c = blockIdx.x; c < T; c += gridDim.x) {
-    if (threadIdx.x == 0) {
-      // last o with piece_base[o] <= c
-      uint32_t lo = 0, hi = K;
-      while (lo < hi) {
-        const uint32_t mid = (lo + hi) >> 1;
-        if (piece_base[mid] <= c) lo = mid + 1;
-        else hi = mid;
-      }
-      s_key = lo - 1;
+  const uint32_t per = (uint32_t)ceil_div(T, gridDim.x);
+  const uint64_t first = (uint64_t)blockIdx.x * per;
+  if (first >= T) return;  // no pieces left for this CTA
+  const uint32_t c0 = (uint32_t)first;
+  const uint32_t c1 = T - c0 < per ? T : c0 + per;
+  if (threadIdx.x == 0) {
+    uint32_t lo = 0, hi = K;
+    while (lo < hi) {
+      const uint32_t mid = (lo + hi) >> 1;
+      if (piece_base[mid] <= c0) lo = mid + 1;
+      else hi = mid;
     }
-    __syncthreads();
-    const uint32_t o = s_key;
-    __syncthreads();
+    s_key = lo - 1;
+  }
+  __syncthreads();
+  uint32_t o = s_key;
+  for (uint32_t c = c0; c < c1; ++c) {
+    while (o + 1 < K && piece_base[o + 1] <= c) ++o;
     const KeyParts k = key_parts(in, ends, src_a[o], src_b[o], status);
     const uint32_t na = (uint32_t)ceil_div(k.a_len, kPiece);
     const uint32_t local = c - piece_base[o];
@@ -258,12 +333,22 @@ __global__ void __launch_bounds__(kAThreads) k_copy_pieces(
       dst = out_index + dst0 + k.a_len + (k.gap ? 1u : 0u) + off;
       len = k.b_len - off < kPiece ? k.b_len - off : kPiece;
     }
-    for (uint32_t i = threadIdx.x; i < len; i += kAThreads) dst[i] = src[i];
+    uint32_t v[kPieceItems];
+#pragma unroll
+    for (uint32_t j = 0; j < kPieceItems; ++j) {
+      const uint32_t i = j * kAThreads + threadIdx.x;
+      if (i < len) v[j] = src[i];
+    }
+#pragma unroll
+    for (uint32_t j = 0; j < kPieceItems; ++j) {
+      const uint32_t i = j * kAThreads + threadIdx.x;
+      if (i < len) dst[i] = v[j];
+    }
   }
 }
 
 // Gap words (keys with a B part and a non-zero gap), and keys with no piece.
-__global__ void k_gap_words(AppendIn in, const uint32_t* ends, const uint32_t* src_a,
+__global__ void k_gap_words(AppendIn in, const unsigned long long* ends, const uint32_t* src_a,
                             const uint32_t* src_b, const uint32_t* out_count,
                             const uint32_t* out_offsets, uint32_t* out_index, uint32_t* status) {
   const uint32_t K = *out_count;
@@ -294,8 +379,8 @@ __global__ void k_set_u32(uint32_t* p, uint32_t v) {
 
 // Workspace layout of one append.
 struct AppendWs {
-  WalkWs walk;
-  uint32_t *ends, *b_pos, *b_rank, *src_a, *src_b, *words, *pieces, *sums, *scalars;
+  unsigned long long* ends;
+  uint32_t *b_pos, *b_rank, *src_a, *src_b, *words, *pieces, *sums, *scalars;
   size_t bytes;
 };
 
@@ -307,10 +392,8 @@ AppendWs append_layout(unsigned char* base, uint64_t ka, uint64_t kb) {
     off += align_up(bytes);
     return p;
   };
-  unsigned char* wk = take(walk_bytes());
-  w.walk = base ? walk_ws(wk) : WalkWs{nullptr, nullptr};
   const uint64_t kc = ka + kb;
-  w.ends = reinterpret_cast<uint32_t*>(take((ka + 1) * 4));
+  w.ends = reinterpret_cast<unsigned long long*>(take((ka + 1) * 8));
   w.b_pos = reinterpret_cast<uint32_t*>(take((kb + 1) * 4));
   w.b_rank = reinterpret_cast<uint32_t*>(take((kb + 1) * 4));
   w.src_a = reinterpret_cast<uint32_t*>(take((kc + 1) * 4));
@@ -366,9 +449,12 @@ int wah_append(const uint32_t* a_keys, const uint32_t* a_offsets, const uint32_t
   uint32_t launches = 0;
   cudaError_t e = cudaMemsetAsync(w.scalars, 0, 16 * 4, s);
   // 1. end chunk of every A key
-  if (e == cudaSuccess && keycnt_a) {
-    WalkIn win{a_keys, a_offsets, a_index, keycnt_a, index_len_a};
-    e = enqueue_walk(win, 0u, 0xFFFFFFFFu, w.walk, KeyEndAct{w.ends}, s, &launches);
+  if (e == cudaSuccess && keycnt_a) e = cudaMemsetAsync(w.ends, 0, (size_t)keycnt_a * 8, s);
+  if (e == cudaSuccess && keycnt_a && index_len_a) {
+    const uint64_t tiles = ceil_div(index_len_a, kEndTile);
+    k_key_ends<<<(unsigned)std::min<uint64_t>(tiles, (uint64_t)grid * 2), 256, 0, s>>>(
+        a_offsets, a_index, keycnt_a, index_len_a, w.ends);
+    ++launches;
   }
   // 2. the merged key set: K = ka + B keys new to A
   if (e == cudaSuccess && kc) e = cudaMemsetAsync(w.src_a, 0xFF, kc * 4, s);

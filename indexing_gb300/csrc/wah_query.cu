@@ -57,7 +57,6 @@ struct DecodeAct {
   uint64_t n;
   uint32_t* status;
   static constexpr bool kNeedsValue = true;
-  static constexpr bool kWantsEnds = false;
   __device__ __forceinline__ void head(uint32_t key, uint32_t pos) const {
     if (key_rows) key_rows[key] = pos;
   }
@@ -85,7 +84,6 @@ struct ExpandAct {
   uint64_t nchunks;
   uint32_t* status;
   static constexpr bool kNeedsValue = false;
-  static constexpr bool kWantsEnds = false;
   __device__ __forceinline__ void head(uint32_t, uint32_t) const {}
   __device__ __forceinline__ void literal(uint32_t, uint32_t chunk, uint32_t bits, uint32_t) const {
     if (chunk >= nchunks) {

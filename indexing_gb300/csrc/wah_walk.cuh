@@ -368,9 +368,6 @@ __global__ void __launch_bounds__(kQThreads) k_walk_emit(WalkIn in, const Span* 
     // literal of the new key, so keys[] is read only for valid keys
     uint32_t key = kcur + h0;
     uint32_t value = 0, value_key = kNone;
-    // actions that want each key's end chunk: the word before the next
-    // key's head (or the span's last word) ends a key
-    uint32_t end_key = kNone, next_head = kNone;
     {
       uint32_t h = h0;
 #pragma unroll
@@ -393,13 +390,6 @@ __global__ void __launch_bounds__(kQThreads) k_walk_emit(WalkIn in, const Span* 
           chunk += 1;
         } else {
           chunk += x & kFillMask;
-        }
-        if constexpr (Act::kWantsEnds) {
-          if (key != end_key) {
-            end_key = key;
-            next_head = key + 1 < S.kb ? in.offsets[key + 1] : S.w1;
-          }
-          if (p + q + 1 == next_head) act.key_end(key, chunk);
         }
       }
     }
