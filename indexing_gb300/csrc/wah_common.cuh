@@ -60,14 +60,13 @@ constexpr int kSelA = 1;
 constexpr int kSelB = 2;
 
 struct WahCtrl {
-  uint32_t hist[kDigits][kRadix];     // rows per digit value, per pass
-  uint32_t bin_off[kDigits][kRadix];  // exclusive scan of hist
   int32_t pass_src[kDigits];          // -1: pass skipped (trivial digit)
   int32_t pass_dst[kDigits];
   int32_t final_sel;                  // where the sorted stream ends up
   uint32_t tile_ctr[8];               // [0..3] sort passes, [4] build
   uint32_t key_or;                    // OR of all keys (range check vs bound)
-  uint32_t pad[2];
+  uint32_t key_nor;                   // OR of the complements: bits some key has clear
+  uint32_t pad[1];
 };
 
 

@@ -9,15 +9,16 @@
 // scatter CTAs); each range is owned by one persistent CTA, so no CTA ever
 // waits for another:
 //
-//   k_digit_histogram  one read of the keys (128-bit loads): histograms of
-//                      every digit the bound allows for the whole column, the
-//                      digit-0 histogram per range, and the OR of all keys
-//   k_sort_plan        bin offsets per digit, trivial digits skipped, homes
+//   k_digit_histogram  one read of the keys (128-bit loads): the digit-0
+//                      histogram per range, the OR of all keys and the OR of
+//                      their complements
+//   k_sort_plan        trivial digits (every key shares them) skipped, homes
 //                      of each pass
 //   k_range_count      for digit passes after the first: per-range histogram
 //                      of the digit over the current order (one read of keys)
-//   k_range_scan       start of every (range, bin) = bin offset + counts of
-//                      the same bin in earlier ranges
+//   k_range_scan       start of every (range, bin) = bin offset (a scan of
+//                      the bins' totals over all ranges) + counts of the same
+//                      bin in earlier ranges
 //   k_radix_scatter    per range, tile after tile: the next tile's keys and
 //                      row ids are fetched by cp.async.bulk into shared memory
 //                      while this one is ranked (warp peer masks, stable per
@@ -40,10 +41,12 @@ template <int DIGITS>
 struct WarpHist {
   uint32_t (*h)[kRadix];  // this warp's private [DIGITS][256] counters
   int first;              // digit of h[0]
-  __device__ __forceinline__ void add_full_warp(uint32_t x, uint32_t lane, uint32_t& acc_or) {
+  __device__ __forceinline__ void add_full_warp(uint32_t x, uint32_t lane, uint32_t& acc_or,
+                                                uint32_t& acc_nor) {
     const uint32_t o = __reduce_or_sync(0xffffffffu, x);
     const uint32_t a = __reduce_and_sync(0xffffffffu, x);
     acc_or |= o;
+    acc_nor |= ~a;
     const uint32_t varying = o ^ a;
 #pragma unroll
     for (int p = 0; p < DIGITS; ++p) {
@@ -55,8 +58,9 @@ struct WarpHist {
       }
     }
   }
-  __device__ __forceinline__ void add_one(uint32_t x, uint32_t& acc_or) {
+  __device__ __forceinline__ void add_one(uint32_t x, uint32_t& acc_or, uint32_t& acc_nor) {
     acc_or |= x;
+    acc_nor |= ~x;
 #pragma unroll
     for (int p = 0; p < DIGITS; ++p)
       atomicAdd(&h[p][digit8(x, first + p)], 1u);
@@ -64,15 +68,16 @@ struct WarpHist {
 };
 
 // Histogram of keys[lo, hi) for digits first..first+DIGITS-1 into the
-// block-shared s_h[warp][DIGITS][256]; returns the warp's OR of the keys.
+// block-shared s_h[warp][DIGITS][256]; returns the warp's OR of the keys and
+// OR of their complements (the bits some key has clear).
 template <int DIGITS>
-__device__ __forceinline__ uint32_t histogram_range(const uint32_t* __restrict__ keys, uint64_t lo,
+__device__ __forceinline__ uint2 histogram_range(const uint32_t* __restrict__ keys, uint64_t lo,
                                                     uint64_t hi, int first,
                                                     uint32_t (*s_h)[DIGITS][kRadix]) {
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const uint32_t nwarps = blockDim.x >> 5;
   WarpHist<DIGITS> wh{s_h[warp], first};
-  uint32_t acc_or = 0;
+  uint32_t acc_or = 0, acc_nor = 0;
   // lo is a multiple of 4 (ranges are whole tiles), so keys + lo is 16-byte
   // aligned.  Work unit: 32 consecutive uint4 (128 keys), one per lane.
   const uint4* kv = reinterpret_cast<const uint4*>(keys + lo);
@@ -85,23 +90,24 @@ __device__ __forceinline__ uint32_t histogram_range(const uint32_t* __restrict__
     for (int u = 0; u < kHistUnroll; ++u) q[u] = ld_stream_v4(kv + (c + u * nwarps) * 32 + lane);
 #pragma unroll
     for (int u = 0; u < kHistUnroll; ++u) {
-      wh.add_full_warp(q[u].x, lane, acc_or);
-      wh.add_full_warp(q[u].y, lane, acc_or);
-      wh.add_full_warp(q[u].z, lane, acc_or);
-      wh.add_full_warp(q[u].w, lane, acc_or);
+      wh.add_full_warp(q[u].x, lane, acc_or, acc_nor);
+      wh.add_full_warp(q[u].y, lane, acc_or, acc_nor);
+      wh.add_full_warp(q[u].z, lane, acc_or, acc_nor);
+      wh.add_full_warp(q[u].w, lane, acc_or, acc_nor);
     }
   }
   for (; c < chunks; c += nwarps) {
     const uint4 q = ld_stream_v4(kv + c * 32 + lane);
-    wh.add_full_warp(q.x, lane, acc_or);
-    wh.add_full_warp(q.y, lane, acc_or);
-    wh.add_full_warp(q.z, lane, acc_or);
-    wh.add_full_warp(q.w, lane, acc_or);
+    wh.add_full_warp(q.x, lane, acc_or, acc_nor);
+    wh.add_full_warp(q.y, lane, acc_or, acc_nor);
+    wh.add_full_warp(q.z, lane, acc_or, acc_nor);
+    wh.add_full_warp(q.w, lane, acc_or, acc_nor);
   }
   // Ragged end (< 128 keys): warp 0, one key per lane.
   if (warp == 0)
-    for (uint64_t i = lo + chunks * 128 + lane; i < hi; i += 32) wh.add_one(keys[i], acc_or);
-  return __reduce_or_sync(0xffffffffu, acc_or);
+    for (uint64_t i = lo + chunks * 128 + lane; i < hi; i += 32)
+      wh.add_one(keys[i], acc_or, acc_nor);
+  return make_uint2(__reduce_or_sync(0xffffffffu, acc_or), __reduce_or_sync(0xffffffffu, acc_nor));
 }
 
 // Part q of a range: the rows one counting CTA covers (parts start on
@@ -113,29 +119,31 @@ __device__ __forceinline__ void sub_range(const RangeView& rv, uint32_t q, uint6
   *hi = q + 1 == kCountCtasPerRange ? rv.hi : *lo + part;
 }
 
-template <int DIGITS, class G>
+// One read of the keys: per-range counts of digit 0, and the OR of the keys
+// and of their complements (which digits vary at all).  Later digits are
+// counted per range by k_range_count over the order they are sorted from.
+template <class G>
 __global__ void __launch_bounds__(kHistThreads)
     k_digit_histogram(G g, uint32_t* __restrict__ range_hist0) {
-  __shared__ uint32_t s_h[kHistWarps][DIGITS][kRadix];
-  for (int i = threadIdx.x; i < kHistWarps * DIGITS * kRadix; i += kHistThreads)
-    (&s_h[0][0][0])[i] = 0;
+  __shared__ uint32_t s_h[kHistWarps][1][kRadix];
+  for (int i = threadIdx.x; i < kHistWarps * kRadix; i += kHistThreads) (&s_h[0][0][0])[i] = 0;
   __syncthreads();
   const uint32_t r = blockIdx.x / kCountCtasPerRange;
   const RangeView rv = g.range(r);
   const ColumnView c = g.col(rv.col);
   uint64_t lo, hi;
   sub_range(rv, blockIdx.x % kCountCtasPerRange, &lo, &hi);
-  const uint32_t acc_or = histogram_range<DIGITS>(c.input, lo, hi, 0, s_h);
-  if ((threadIdx.x & 31) == 0 && acc_or) atomicOr(&c.ctrl->key_or, acc_or);
+  const uint2 acc = histogram_range<1>(c.input, lo, hi, 0, s_h);
+  if ((threadIdx.x & 31) == 0) {
+    if (acc.x) atomicOr(&c.ctrl->key_or, acc.x);
+    if (acc.y) atomicOr(&c.ctrl->key_nor, acc.y);
+  }
   __syncthreads();
-  for (int j = threadIdx.x; j < DIGITS * kRadix; j += kHistThreads) {
+  for (int j = threadIdx.x; j < kRadix; j += kHistThreads) {
     uint32_t s = 0;
 #pragma unroll
-    for (int w = 0; w < kHistWarps; ++w) s += (&s_h[w][0][0])[j];
-    if (s) {
-      atomicAdd(&(&c.ctrl->hist[0][0])[j], s);
-      if (j < kRadix) atomicAdd(&range_hist0[(uint64_t)r * kRadix + j], s);
-    }
+    for (int w = 0; w < kHistWarps; ++w) s += s_h[w][0][j];
+    if (s) atomicAdd(&range_hist0[(uint64_t)r * kRadix + j], s);
   }
 }
 
@@ -169,24 +177,15 @@ __global__ void __launch_bounds__(kHistThreads)
 // ---------------------------------------------------------------------------
 template <class G>
 __global__ void __launch_bounds__(kRadix) k_sort_plan(G g) {
-  __shared__ uint32_t s_warp[kRadix / 32 + 1];
-  __shared__ int s_active[kDigits];
   const ColumnView c = g.col(blockIdx.x);
   WahCtrl* ctrl = c.ctrl;
-  const uint64_t n = c.n;
   const int passes = c.passes;
   uint32_t* status = c.status;
-  const int b = threadIdx.x;
-  for (int p = 0; p < passes; ++p) {
-    const uint32_t h = ctrl->hist[p][b];
-    const int trivial = __syncthreads_or(h == (uint32_t)n);
-    uint32_t total;
-    const uint32_t excl = block_exclusive_scan<kRadix>(h, &total, s_warp);
-    ctrl->bin_off[p][b] = excl;
-    if (b == 0) s_active[p] = !trivial;
-  }
-  __syncthreads();
-  if (b == 0) {
+  if (threadIdx.x == 0) {
+    // a digit every key shares is trivial: one bin, order unchanged
+    const uint32_t varying = ctrl->key_or & ctrl->key_nor;
+    int s_active[kDigits];
+    for (int p = 0; p < kDigits; ++p) s_active[p] = digit8(varying, p) != 0;
     // A set bit above the digits the bound allows: the sort would be wrong.
     if (passes < kDigits && (ctrl->key_or >> (passes * kRadixBits)) != 0)
       set_status(status, WAH_ERANGE);
@@ -206,17 +205,25 @@ __global__ void __launch_bounds__(kRadix) k_sort_plan(G g) {
   }
 }
 
-// Start of every (range, bin) of one column for one pass.
+// Start of every (range, bin) of one column for one pass: the bin's offset
+// (rows of smaller digits in all ranges) plus the bin's rows in earlier
+// ranges.
 template <class G>
 __global__ void __launch_bounds__(kRadix)
     k_range_scan(G g, int pass, const uint32_t* __restrict__ range_hist,
                  uint32_t* __restrict__ range_start) {
+  __shared__ uint32_t s_warp[kRadix / 32 + 1];
   const ColumnView col = g.col(blockIdx.x);
   if (col.ctrl->pass_src[pass] < 0) return;
   const uint32_t b = threadIdx.x;
-  uint32_t run = col.ctrl->bin_off[pass][b];
-  uint32_t c = g.first_range(blockIdx.x);
+  const uint32_t c0 = g.first_range(blockIdx.x);
   const uint32_t end = g.end_range(blockIdx.x);
+  uint32_t total = 0;
+#pragma unroll 8
+  for (uint32_t c = c0; c < end; ++c) total += range_hist[(uint64_t)c * kRadix + b];
+  uint32_t all;
+  uint32_t run = block_exclusive_scan<kRadix>(total, &all, s_warp);
+  uint32_t c = c0;
   for (; c + 8 <= end; c += 8) {
     uint32_t h[8];
 #pragma unroll
@@ -521,12 +528,7 @@ cudaError_t launch_sort_t(const G& g, uint32_t ncols, uint32_t ranges, const Ran
       cudaMemsetAsync(ra.hist, 0, (size_t)kDigits * ra.max_ranges * kRadix * 4, s);
   if (err != cudaSuccess) return err;
   record_phase(o.events, kPhaseHist, false, s);
-  switch (o.max_passes) {
-    case 1: k_digit_histogram<1, G><<<count_grid, kHistThreads, 0, s>>>(g, ra.hist); break;
-    case 2: k_digit_histogram<2, G><<<count_grid, kHistThreads, 0, s>>>(g, ra.hist); break;
-    case 3: k_digit_histogram<3, G><<<count_grid, kHistThreads, 0, s>>>(g, ra.hist); break;
-    default: k_digit_histogram<4, G><<<count_grid, kHistThreads, 0, s>>>(g, ra.hist); break;
-  }
+  k_digit_histogram<G><<<count_grid, kHistThreads, 0, s>>>(g, ra.hist);
   record_phase(o.events, kPhaseHist, true, s);
   ++*launches;
   record_phase(o.events, kPhasePlan, false, s);
