@@ -1,12 +1,12 @@
 // wah_walk.cuh -- the device-wide walk over a run of keys' WAH words.
 //
-// Shared by the decoder and queries (wah_query.cu) and by incremental
-// appends (wah_append.cu).  For every word of keys [ka, kb) it knows the
-// word's key, the chunk position of the word within its key (a segmented
-// exclusive scan of chunk advances: 1 per literal, the count of a fill) and
-// the number of rows in all earlier words (a plain exclusive scan of the
-// literals' popcounts), and hands every literal -- and, for actions that ask,
-// every key's end chunk -- to an action.  Look-back free: the words are cut
+// Used by the decoder and queries (wah_query.cu); incremental appends
+// (wah_append.cu) take only its word constants and chunk_advance.  For every
+// word of keys [ka, kb) it knows the word's key, the chunk position of the
+// word within its key (a segmented exclusive scan of chunk advances: 1 per
+// literal, the count of a fill) and the number of rows in all earlier words
+// (a plain exclusive scan of the literals' popcounts), and hands every
+// literal to an action.  Look-back free: the words are cut
 // into equal ranges, one persistent CTA per range; k_walk_count reduces each
 // range, k_walk_scan scans the range aggregates, k_walk_emit re-reads the
 // range tile by tile with the carries.
