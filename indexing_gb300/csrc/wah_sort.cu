@@ -207,24 +207,45 @@ __global__ void __launch_bounds__(kRadix) k_sort_plan(G g) {
 
 // Start of every (range, bin) of one column for one pass: the bin's offset
 // (rows of smaller digits in all ranges) plus the bin's rows in earlier
-// ranges.
+// ranges.  Four threads per bin, each over a quarter of the ranges.
+constexpr int kRangeScanParts = 4;
+constexpr int kRangeScanThreads = kRadix * kRangeScanParts;
+
 template <class G>
-__global__ void __launch_bounds__(kRadix)
+__global__ void __launch_bounds__(kRangeScanThreads)
     k_range_scan(G g, int pass, const uint32_t* __restrict__ range_hist,
                  uint32_t* __restrict__ range_start) {
-  __shared__ uint32_t s_warp[kRadix / 32 + 1];
+  __shared__ uint32_t s_warp[kRangeScanThreads / 32 + 1];
+  __shared__ uint32_t s_part[kRangeScanParts][kRadix];
   const ColumnView col = g.col(blockIdx.x);
   if (col.ctrl->pass_src[pass] < 0) return;
-  const uint32_t b = threadIdx.x;
+  const uint32_t b = threadIdx.x % kRadix, q = threadIdx.x / kRadix;
   const uint32_t c0 = g.first_range(blockIdx.x);
   const uint32_t end = g.end_range(blockIdx.x);
-  uint32_t total = 0;
+  const uint32_t per = (end - c0 + kRangeScanParts - 1) / kRangeScanParts;
+  const uint32_t lo = c0 + q * per < end ? c0 + q * per : end;
+  const uint32_t hi = lo + per < end ? lo + per : end;
+  uint32_t part = 0;
 #pragma unroll 8
-  for (uint32_t c = c0; c < end; ++c) total += range_hist[(uint64_t)c * kRadix + b];
+  for (uint32_t c = lo; c < hi; ++c) part += range_hist[(uint64_t)c * kRadix + b];
+  s_part[q][b] = part;
+  __syncthreads();
+  uint32_t total = 0, before = 0;
+#pragma unroll
+  for (int k = 0; k < kRangeScanParts; ++k) {
+    const uint32_t x = s_part[k][b];
+    if (k < (int)q) before += x;
+    total += x;
+  }
+  // threads of part 0 carry the bins' totals through the scan, the others 0
   uint32_t all;
-  uint32_t run = block_exclusive_scan<kRadix>(total, &all, s_warp);
-  uint32_t c = c0;
-  for (; c + 8 <= end; c += 8) {
+  const uint32_t off = block_exclusive_scan<kRangeScanThreads>(q == 0 ? total : 0u, &all, s_warp);
+  __syncthreads();
+  if (q == 0) s_part[0][b] = off;
+  __syncthreads();
+  uint32_t run = s_part[0][b] + before;
+  uint32_t c = lo;
+  for (; c + 8 <= hi; c += 8) {
     uint32_t h[8];
 #pragma unroll
     for (int u = 0; u < 8; ++u) h[u] = range_hist[(uint64_t)(c + u) * kRadix + b];
@@ -234,7 +255,7 @@ __global__ void __launch_bounds__(kRadix)
       run += h[u];
     }
   }
-  for (; c < end; ++c) {
+  for (; c < hi; ++c) {
     range_start[(uint64_t)c * kRadix + b] = run;
     run += range_hist[(uint64_t)c * kRadix + b];
   }
@@ -551,7 +572,7 @@ cudaError_t launch_sort_t(const G& g, uint32_t ncols, uint32_t ranges, const Ran
       k_range_count<G><<<count_grid, kHistThreads, 0, s>>>(g, p, rh);
       ++*launches;
     }
-    k_range_scan<G><<<ncols, kRadix, 0, s>>>(g, p, rh, ra.start);
+    k_range_scan<G><<<ncols, kRangeScanThreads, 0, s>>>(g, p, rh, ra.start);
     ++*launches;
     record_phase(o.events, kPhaseScatter0 + p, false, s);
     v.fn<<<ranges, kSortThreads, v.smem, s>>>(g, p, ra.start);
