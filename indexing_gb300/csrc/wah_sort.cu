@@ -32,38 +32,21 @@
 namespace wah {
 
 // ---------------------------------------------------------------------------
-// Digit histograms.  Per warp and key slot, a digit whose 8 bits agree across
-// all 32 lanes (found from the warp's OR and AND of the keys) is counted with
-// one shared atomic for the warp instead of 32: constant high digits of small
-// keys and runs of equal values cost almost nothing.
+// Digit histograms: one shared atomic per key and digit into the warp's
+// private counters.  (Counting a digit the whole warp shares once per warp,
+// found from the warp's OR and AND of the keys, measured slower on every
+// distribution, run-clustered ones included: the two warp reductions per key
+// cost more than the same-address atomics they save.)
 // ---------------------------------------------------------------------------
 template <int DIGITS>
 struct WarpHist {
   uint32_t (*h)[kRadix];  // this warp's private [DIGITS][256] counters
   int first;              // digit of h[0]
-  __device__ __forceinline__ void add_full_warp(uint32_t x, uint32_t lane, uint32_t& acc_or,
-                                                uint32_t& acc_nor) {
-    const uint32_t o = __reduce_or_sync(0xffffffffu, x);
-    const uint32_t a = __reduce_and_sync(0xffffffffu, x);
-    acc_or |= o;
-    acc_nor |= ~a;
-    const uint32_t varying = o ^ a;
-#pragma unroll
-    for (int p = 0; p < DIGITS; ++p) {
-      const uint32_t d = digit8(x, first + p);
-      if (digit8(varying, first + p) == 0) {
-        if (lane == 0) atomicAdd(&h[p][d], 32u);
-      } else {
-        atomicAdd(&h[p][d], 1u);
-      }
-    }
-  }
-  __device__ __forceinline__ void add_one(uint32_t x, uint32_t& acc_or, uint32_t& acc_nor) {
+  __device__ __forceinline__ void add(uint32_t x, uint32_t& acc_or, uint32_t& acc_nor) {
     acc_or |= x;
     acc_nor |= ~x;
 #pragma unroll
-    for (int p = 0; p < DIGITS; ++p)
-      atomicAdd(&h[p][digit8(x, first + p)], 1u);
+    for (int p = 0; p < DIGITS; ++p) atomicAdd(&h[p][digit8(x, first + p)], 1u);
   }
 };
 
@@ -90,23 +73,23 @@ __device__ __forceinline__ uint2 histogram_range(const uint32_t* __restrict__ ke
     for (int u = 0; u < kHistUnroll; ++u) q[u] = ld_stream_v4(kv + (c + u * nwarps) * 32 + lane);
 #pragma unroll
     for (int u = 0; u < kHistUnroll; ++u) {
-      wh.add_full_warp(q[u].x, lane, acc_or, acc_nor);
-      wh.add_full_warp(q[u].y, lane, acc_or, acc_nor);
-      wh.add_full_warp(q[u].z, lane, acc_or, acc_nor);
-      wh.add_full_warp(q[u].w, lane, acc_or, acc_nor);
+      wh.add(q[u].x, acc_or, acc_nor);
+      wh.add(q[u].y, acc_or, acc_nor);
+      wh.add(q[u].z, acc_or, acc_nor);
+      wh.add(q[u].w, acc_or, acc_nor);
     }
   }
   for (; c < chunks; c += nwarps) {
     const uint4 q = ld_stream_v4(kv + c * 32 + lane);
-    wh.add_full_warp(q.x, lane, acc_or, acc_nor);
-    wh.add_full_warp(q.y, lane, acc_or, acc_nor);
-    wh.add_full_warp(q.z, lane, acc_or, acc_nor);
-    wh.add_full_warp(q.w, lane, acc_or, acc_nor);
+    wh.add(q.x, acc_or, acc_nor);
+    wh.add(q.y, acc_or, acc_nor);
+    wh.add(q.z, acc_or, acc_nor);
+    wh.add(q.w, acc_or, acc_nor);
   }
   // Ragged end (< 128 keys): warp 0, one key per lane.
   if (warp == 0)
     for (uint64_t i = lo + chunks * 128 + lane; i < hi; i += 32)
-      wh.add_one(keys[i], acc_or, acc_nor);
+      wh.add(keys[i], acc_or, acc_nor);
   return make_uint2(__reduce_or_sync(0xffffffffu, acc_or), __reduce_or_sync(0xffffffffu, acc_nor));
 }
 
