@@ -19,14 +19,24 @@
 // default 1023 = 33 x 31).
 //
 // Flags as the reference (-f, -b bound, -d device name, -p print,
-// --batch-size, -j/--jobs, -w/--work-groups) plus --output FILE and
-// --host-parse (the data file is parsed on the GPU by default).  Prints the
-// reference's lines ('N' values, maximum value, device, -p listing of keys
-// 0..bound, Time: 'X' ms).
+// --batch-size, -j/--jobs, -w/--work-groups) plus --output FILE,
+// --host-parse (the data file is parsed on the GPU by default) and
+// --device-merge (slices are appended to one index on the GPU with
+// wah_append, in row order, and the merged index comes back once; the
+// merger takes it whole).  Prints the reference's lines ('N' values, maximum
+// value, device, -p listing of keys 0..bound, Time: 'X' ms).
+//
+// As in the reference, the clock starts when the merger is initialised,
+// after the worker exists: the column is staged in page-locked memory and the
+// worker's device and page-locked buffers are set up before that; batches
+// are sent as row spans of the staged column and copied to the device from
+// there.
 #include <algorithm>
 #include <cstdio>
+#include <cstring>
 #include <deque>
 #include <map>
+#include <memory>
 #include <string>
 #include <thread>
 #include <type_traits>
@@ -47,6 +57,7 @@ struct work_atom {};
 struct done_atom {};
 struct add_atom {};
 struct quit_atom {};
+struct ready_atom {};
 
 constexpr uint32_t kChunk = 31;
 
@@ -58,7 +69,29 @@ struct slice_index {
   uint32_t n = 0;
   int status = WAH_OK;
   std::vector<uint32_t> keys, offsets, index;
+  // The whole column's index merged on the device: its arrays stay in the
+  // page-locked block `hold` (no copy into the vectors above).
+  bool whole = false;
+  std::shared_ptr<uint32_t> hold;
+  const uint32_t *pk = nullptr, *po = nullptr, *pw = nullptr;
+  uint32_t kc = 0, wc = 0;
 };
+
+// -p listing of keys 0..bound from a (keys, offsets, index) triple
+// (src/gpu.cpp:153-158 prints every key up to the bound).
+void print_keys_upto(uint32_t bound, const uint32_t* keys, const uint32_t* offsets, uint32_t K,
+                     const uint32_t* words, uint32_t L) {
+  uint32_t i = 0;
+  for (uint64_t key = 0; key <= bound; ++key) {
+    while (i < K && keys[i] < key) ++i;
+    std::string bits;
+    if (i < K && keys[i] == key) {
+      const uint32_t end = i + 1 < K ? offsets[i + 1] : L;
+      bits = wahcli::decoded_bitmap(words + offsets[i], end - offsets[i]);
+    }
+    std::printf("%llu\t%s\n", (unsigned long long)key, bits.c_str());
+  }
+}
 
 // ---------------------------------------------------------------- merger --
 
@@ -69,6 +102,8 @@ struct merger_state {
   std::chrono::steady_clock::time_point start;
   wahmerge::slice_merger index{std::min(16u, std::max(1u, std::thread::hardware_concurrency()))};
   std::map<uint64_t, slice_index> pending;  // slices that arrived early
+  slice_index whole;                         // --device-merge: the merged index
+  bool have_whole = false;
   int status = WAH_OK;
   int* exit_code = nullptr;
 };
@@ -89,6 +124,11 @@ behavior merger(actor_ctx<merger_state>& self) {
           if (s.status == WAH_OK) s.status = x.status;
           return;
         }
+        if (x.whole) {  // merged on the device already
+          s.whole = std::move(x);
+          s.have_whole = true;
+          return;
+        }
         // slices are merged in row order
         s.pending.emplace(x.row_start, std::move(x));
         while (!s.pending.empty() && s.pending.begin()->first == s.index.rows()) {
@@ -107,6 +147,18 @@ behavior merger(actor_ctx<merger_state>& self) {
         if (s.status != WAH_OK) {
           std::fprintf(stderr, "[!!!] %s\n", wah_strerror(s.status));
           *s.exit_code = 1;
+          self.quit();
+          return;
+        }
+        if (s.have_whole) {
+          const slice_index& x = s.whole;
+          if (s.print_results) print_keys_upto(s.bound, x.pk, x.po, x.kc, x.pw, x.wc);
+          std::printf("Index has %u elements with %u keys\n", x.wc, x.kc);
+          std::printf("Time: '%llu' ms\n", (unsigned long long)ms);
+          if (!s.output.empty() && !wahcli::write_result(s.output, x.pk, x.po, x.kc, x.pw, x.wc)) {
+            std::fprintf(stderr, "cannot write '%s'\n", s.output.c_str());
+            *s.exit_code = 1;
+          }
           self.quit();
           return;
         }
@@ -139,7 +191,7 @@ struct job_slot {
   void* stream = nullptr;
   uint32_t *d_values = nullptr, *d_keys = nullptr, *d_offsets = nullptr, *d_index = nullptr;
   wah_counts* d_counts = nullptr;
-  uint32_t *h_values = nullptr, *h_keys = nullptr, *h_offsets = nullptr, *h_index = nullptr;
+  uint32_t *h_keys = nullptr, *h_offsets = nullptr, *h_index = nullptr;
   wah_counts* h_counts = nullptr;
   void* ws = nullptr;  // one slice per batch: wah_build's workspace
   wah_batch* batch = nullptr;
@@ -158,6 +210,20 @@ struct worker_state {
   uint32_t wg_size = 0, wg_num = 0, bound = 0;
   uint64_t v_stride = 0, k_stride = 0, i_stride = 0;
   size_t ws_bytes = 0;
+  const uint32_t* input = nullptr;  // the column, page-locked
+  uint64_t total_rows = 0;
+  // --device-merge: the index of rows [0, acc_rows) in acc_*[acc_cur]
+  bool device_merge = false;
+  uint32_t *acc_k[2] = {nullptr, nullptr}, *acc_o[2] = {nullptr, nullptr};
+  uint32_t* acc_w[2] = {nullptr, nullptr};
+  wah_counts* acc_counts = nullptr;    // device
+  wah_counts* h_acc_counts = nullptr;  // page-locked
+  uint64_t acc_rows = 0, acc_keys_cap = 0, acc_index_cap = 0;
+  uint32_t acc_K = 0, acc_L = 0;
+  int acc_cur = 0;
+  void* app_ws = nullptr;
+  size_t app_ws_bytes = 0;
+  std::shared_ptr<uint32_t> out_hold;  // page-locked keys | offsets | words
   std::vector<job_slot> slots;
   actor reply_to;
   // completion thread: waits for batches in submission order
@@ -196,13 +262,78 @@ struct worker_state {
       dev(k_stride * wg_num * 4, &j.d_offsets);
       dev(i_stride * wg_num * 4, &j.d_index);
       dev(sizeof(wah_counts) * wg_num, &j.d_counts);
-      host(v_stride * wg_num * 4, &j.h_values);
-      host(k_stride * wg_num * 4, &j.h_keys);
-      host(k_stride * wg_num * 4, &j.h_offsets);
-      host(i_stride * wg_num * 4, &j.h_index);
+      if (!device_merge) {  // slices come back to the host one by one
+        host(k_stride * wg_num * 4, &j.h_keys);
+        host(k_stride * wg_num * 4, &j.h_offsets);
+        host(i_stride * wg_num * 4, &j.h_index);
+      }
       host(sizeof(wah_counts) * wg_num, &j.h_counts);
       if (wg_num == 1 && rc == WAH_OK) rc = wah_dev_alloc(ws_bytes, &j.ws);
     }
+    if (device_merge && rc == WAH_OK) {
+      // wah_append checks its outputs against ka + kb keys and la + lb + kb
+      // words (one gap word per key of the slice): the merged index's own
+      // bounds plus one slice's keys
+      wah_output_caps(std::max<uint64_t>(total_rows, 1), bound, &acc_keys_cap, &acc_index_cap);
+      acc_keys_cap += k_stride;
+      acc_index_cap = 2 * std::max<uint64_t>(total_rows, 1) + k_stride;
+      for (int b = 0; b < 2; ++b) {
+        dev(acc_keys_cap * 4, &acc_k[b]);
+        dev(acc_keys_cap * 4, &acc_o[b]);
+        dev(acc_index_cap * 4, &acc_w[b]);
+      }
+      dev(sizeof(wah_counts), &acc_counts);
+      host(sizeof(wah_counts), &h_acc_counts);
+      app_ws_bytes = wah_append_workspace_bytes(static_cast<uint32_t>(acc_keys_cap),
+                                                static_cast<uint32_t>(k_stride));
+      if (rc == WAH_OK) rc = wah_dev_alloc(app_ws_bytes, &app_ws);
+      uint32_t* out = nullptr;
+      host((2 * acc_keys_cap + acc_index_cap) * 4, &out);
+      if (out) out_hold = std::shared_ptr<uint32_t>(out, [](uint32_t* q) { wah_host_free(q); });
+    }
+    return rc;
+  }
+
+  // Appends slice c of batch j to the merged index (device, row order).
+  int append_slice(job_slot& j, uint32_t c, const wah_counts& cb) {
+    const int nxt = acc_cur ^ 1;
+    int rc = wah_append(acc_k[acc_cur], acc_o[acc_cur], acc_w[acc_cur], acc_K, acc_L, acc_rows,
+                        j.d_keys + c * k_stride, j.d_offsets + c * k_stride,
+                        j.d_index + c * i_stride, cb.keycnt, cb.index_len, acc_k[nxt],
+                        acc_o[nxt], acc_w[nxt], acc_keys_cap, acc_index_cap, acc_counts, app_ws,
+                        app_ws_bytes, j.stream);
+    if (rc == WAH_OK) rc = wah_copy(h_acc_counts, acc_counts, sizeof(wah_counts), j.stream);
+    if (rc == WAH_OK) rc = wah_stream_sync(j.stream);
+    if (rc == WAH_OK) rc = static_cast<int>(h_acc_counts->status);
+    if (rc == WAH_OK) {
+      acc_K = h_acc_counts->keycnt;
+      acc_L = h_acc_counts->index_len;
+      acc_cur = nxt;
+      acc_rows += j.ns[c];
+    }
+    return rc;
+  }
+
+  // The merged index to page-locked memory, handed on without a copy.
+  int deliver(void* stream, slice_index* x) {
+    uint32_t* k = out_hold.get();
+    uint32_t* o = k + acc_keys_cap;
+    uint32_t* w = o + acc_keys_cap;
+    int rc = WAH_OK;
+    if (acc_K) rc = wah_copy(k, acc_k[acc_cur], uint64_t(acc_K) * 4, stream);
+    if (rc == WAH_OK && acc_K) rc = wah_copy(o, acc_o[acc_cur], uint64_t(acc_K) * 4, stream);
+    if (rc == WAH_OK && acc_L) rc = wah_copy(w, acc_w[acc_cur], uint64_t(acc_L) * 4, stream);
+    if (rc == WAH_OK) rc = wah_stream_sync(stream);
+    x->row_start = 0;
+    x->n = static_cast<uint32_t>(acc_rows);
+    x->status = rc;
+    x->whole = true;
+    x->hold = out_hold;
+    x->pk = k;
+    x->po = o;
+    x->pw = w;
+    x->kc = acc_K;
+    x->wc = acc_L;
     return rc;
   }
 
@@ -221,24 +352,32 @@ struct worker_state {
                       static_cast<void*>(j.d_offsets), static_cast<void*>(j.d_index),
                       static_cast<void*>(j.d_counts), j.ws})
         if (p) wah_dev_free(p);
-      for (void* p : {static_cast<void*>(j.h_values), static_cast<void*>(j.h_keys),
+      for (void* p : {static_cast<void*>(j.h_keys),
                       static_cast<void*>(j.h_offsets), static_cast<void*>(j.h_index),
                       static_cast<void*>(j.h_counts)})
         if (p) wah_host_free(p);
       if (j.batch) wah_batch_destroy(j.batch);
       if (j.stream) wah_stream_destroy(j.stream);
     }
+    for (int b = 0; b < 2; ++b)
+      for (void* p : {static_cast<void*>(acc_k[b]), static_cast<void*>(acc_o[b]),
+                      static_cast<void*>(acc_w[b])})
+        if (p) wah_dev_free(p);
+    if (acc_counts) wah_dev_free(acc_counts);
+    if (app_ws) wah_dev_free(app_ws);
+    if (h_acc_counts) wah_host_free(h_acc_counts);
+    out_hold.reset();  // freed when the merger lets go of it too
     slots.clear();
   }
 
-  // Enqueues one batch: copy in, build every slice, copy the results out.
-  int launch(job_slot& j, const std::vector<uint32_t>& input) {
+  // Enqueues one batch: copy in (from the page-locked column), build every
+  // slice, copy the results out.
+  int launch(job_slot& j) {
     const uint32_t ncols = j.ncols;
-    for (uint32_t c = 0; c < ncols; ++c)
-      std::copy(input.begin() + uint64_t(c) * wg_size,
-                input.begin() + uint64_t(c) * wg_size + j.ns[c], j.h_values + c * v_stride);
-    const uint64_t in_words = uint64_t(ncols - 1) * v_stride + j.ns[ncols - 1];
-    int rc = wah_copy(j.d_values, j.h_values, in_words * 4, j.stream);
+    int rc = WAH_OK;
+    for (uint32_t c = 0; c < ncols && rc == WAH_OK; ++c)
+      rc = wah_copy(j.d_values + c * v_stride, input + j.row_start + uint64_t(c) * wg_size,
+                    uint64_t(j.ns[c]) * 4, j.stream);
     if (rc != WAH_OK) return rc;
     if (wg_num == 1) {
       rc = wah_build(j.d_values, j.ns[0], bound, j.d_keys, j.d_offsets, j.d_index, j.d_counts,
@@ -276,7 +415,7 @@ struct worker_state {
     // one slice: its sizes are read first and exactly K, L words copied
     // (by the completion thread); several: whole capacity regions now
     rc = wah_copy(j.h_counts, j.d_counts, sizeof(wah_counts) * ncols, j.stream);
-    if (rc == WAH_OK && ncols > 1) {
+    if (rc == WAH_OK && ncols > 1 && !device_merge) {
       const uint64_t kw = uint64_t(ncols - 1) * k_stride + std::min<uint64_t>(k_stride, j.ns[ncols - 1]);
       const uint64_t iw = uint64_t(ncols - 1) * i_stride + 2ull * j.ns[ncols - 1];
       rc = wah_copy(j.h_keys, j.d_keys, kw * 4, j.stream);
@@ -300,6 +439,29 @@ struct worker_state {
       job_slot& j = slots[i];
       int rc = j.status;
       if (rc == WAH_OK) rc = wah_stream_sync(j.stream);
+      if (device_merge) {
+        // batches complete in submission order, which is row order
+        std::vector<slice_index> out;
+        for (uint32_t c = 0; c < j.ncols && rc == WAH_OK; ++c) {
+          rc = static_cast<int>(j.h_counts[c].status);
+          if (rc == WAH_OK) rc = append_slice(j, c, j.h_counts[c]);
+        }
+        if (rc != WAH_OK) {
+          out.resize(1);
+          out[0].status = rc;
+        } else if (acc_rows == total_rows) {
+          out.resize(1);
+          deliver(j.stream, &out[0]);
+        }
+        uint64_t processed = 0;
+        for (uint32_t c = 0; c < j.ncols; ++c) processed += j.ns[c];
+        {
+          std::lock_guard<std::mutex> lk(mu);
+          j.busy = false;
+        }
+        sys->send_from(self, reply_to, done_atom{}, processed, std::move(out));
+        continue;
+      }
       if (rc == WAH_OK && j.ncols == 1) {
         const wah_counts c = j.h_counts[0];
         if (c.status == WAH_OK) {
@@ -341,22 +503,28 @@ struct worker_state {
 behavior worker(actor_ctx<worker_state>& self) {
   auto& s = self.state;
   return {
-      handler<init_atom, int, uint32_t, uint32_t, uint32_t, uint32_t, actor>(
-          [&](init_atom, int device, uint32_t jobs, uint32_t wg_size, uint32_t wg_num,
-              uint32_t bound, actor reply_to) {
+      handler_from<init_atom, int, uint32_t, uint32_t, uint32_t, uint32_t, actor, const uint32_t*,
+                   uint64_t, bool>(
+          [&](const actor& from, init_atom, int device, uint32_t jobs, uint32_t wg_size,
+              uint32_t wg_num, uint32_t bound, actor reply_to, const uint32_t* input,
+              uint64_t total_rows, bool device_merge) {
             s.device = device;
             wah_device_select(device);
             s.wg_size = wg_size;
             s.wg_num = wg_num;
             s.bound = bound;
             s.reply_to = reply_to;
+            s.input = input;
+            s.total_rows = total_rows;
+            s.device_merge = device_merge;
             s.sys = &self.system();
             s.self = self.self();
             s.setup_status = s.setup(jobs);
             s.completer = std::thread([&s] { s.complete_loop(); });
+            self.send(from, ready_atom{}, s.setup_status);
           }),
-      handler<work_atom, uint64_t, std::vector<uint32_t>>(
-          [&](work_atom, uint64_t row_start, std::vector<uint32_t> input) {
+      handler<work_atom, uint64_t, uint64_t>(
+          [&](work_atom, uint64_t row_start, uint64_t rows) {
             wah_device_select(s.device);
             size_t i = 0;
             {
@@ -367,15 +535,15 @@ behavior worker(actor_ctx<worker_state>& self) {
             if (i == s.slots.size()) {  // more batches than --jobs: a caller bug
               std::vector<slice_index> err(1);
               err[0].status = WAH_EINVAL;
-              self.send(s.reply_to, done_atom{}, uint64_t(input.size()), std::move(err));
+              self.send(s.reply_to, done_atom{}, rows, std::move(err));
               return;
             }
             job_slot& j = s.slots[i];
             j.row_start = row_start;
-            j.ncols = static_cast<uint32_t>((input.size() + s.wg_size - 1) / s.wg_size);
+            j.ncols = static_cast<uint32_t>((rows + s.wg_size - 1) / s.wg_size);
             j.ns.assign(j.ncols, s.wg_size);
-            j.ns.back() = static_cast<uint32_t>(input.size() - uint64_t(j.ncols - 1) * s.wg_size);
-            j.status = s.setup_status != WAH_OK ? s.setup_status : s.launch(j, input);
+            j.ns.back() = static_cast<uint32_t>(rows - uint64_t(j.ncols - 1) * s.wg_size);
+            j.status = s.setup_status != WAH_OK ? s.setup_status : s.launch(j);
             {
               std::lock_guard<std::mutex> lk(s.mu);
               s.queue.push_back(i);
@@ -394,7 +562,7 @@ behavior worker(actor_ctx<worker_state>& self) {
 
 struct indexer_state {
   actor worker, merger;
-  std::vector<uint32_t> input;
+  uint64_t n = 0;  // rows of the column (staged page-locked, read by the worker)
   uint64_t next_row = 0;   // first row not yet sent
   uint64_t remaining = 0;  // rows not yet indexed
   uint32_t in_progress = 0, jobs = 1, wg_num = 1, wg_size = 1;
@@ -403,37 +571,36 @@ struct indexer_state {
 
 behavior indexer(actor_ctx<indexer_state>& self) {
   auto& s = self.state;
-  auto finish = [&] {
+  // copied into the handlers that call it: this function's frame is gone
+  // by the time they run (the actor's context and state are not)
+  auto finish = [&self, &s] {
     self.send(s.merger, quit_atom{}, s.status);
     self.send(s.worker, quit_atom{});
     self.quit();
   };
   return {
-      handler<init_atom, actor, actor, std::vector<uint32_t>, uint32_t, uint32_t, uint32_t>(
-          [&](init_atom, actor w, actor m, std::vector<uint32_t> input, uint32_t jobs,
-              uint32_t wg_num, uint32_t wg_size) {
+      handler<init_atom, actor, actor, uint64_t, uint32_t, uint32_t, uint32_t>(
+          [&, finish](init_atom, actor w, actor m, uint64_t n, uint32_t jobs, uint32_t wg_num,
+              uint32_t wg_size) {
             s.worker = w;
             s.merger = m;
-            s.remaining = input.size();
-            s.input = std::move(input);
+            s.n = n;
+            s.remaining = n;
             s.jobs = jobs;
             s.wg_num = wg_num;
             s.wg_size = wg_size;
             if (s.remaining == 0) finish();
           }),
       handler<index_atom>([&](index_atom) {
-        if (s.status != WAH_OK || s.in_progress >= s.jobs || s.next_row >= s.input.size()) return;
-        const uint64_t batch = std::min<uint64_t>(s.input.size() - s.next_row,
-                                                  uint64_t(s.wg_size) * s.wg_num);
-        std::vector<uint32_t> slice(s.input.begin() + s.next_row,
-                                    s.input.begin() + s.next_row + batch);
-        self.send(s.worker, work_atom{}, s.next_row, std::move(slice));
+        if (s.status != WAH_OK || s.in_progress >= s.jobs || s.next_row >= s.n) return;
+        const uint64_t batch = std::min<uint64_t>(s.n - s.next_row, uint64_t(s.wg_size) * s.wg_num);
+        self.send(s.worker, work_atom{}, s.next_row, batch);
         s.next_row += batch;
         s.in_progress += 1;
         self.send(self.self(), index_atom{});
       }),
       handler<done_atom, uint64_t, std::vector<slice_index>>(
-          [&](done_atom, uint64_t processed, std::vector<slice_index> slices) {
+          [&, finish](done_atom, uint64_t processed, std::vector<slice_index> slices) {
             s.in_progress -= 1;
             s.remaining -= std::min(processed, s.remaining);
             for (auto& x : slices) {
@@ -454,7 +621,7 @@ behavior indexer(actor_ctx<indexer_state>& self) {
 int main(int argc, char** argv) {
   std::string filename, device_name, output;
   uint32_t bound = 0, batch_size = 1023, jobs = 1, work_groups = 1;
-  bool print_results = false, host_parse = false;
+  bool print_results = false, host_parse = false, device_merge = false;
   const std::vector<wahcli::flag> flags = {
       {"data-file", 'f', "file with test data (one value per line)", wahcli::flag::STRING, &filename},
       {"bound", 'b', "maximum value (0 will scan values)", wahcli::flag::U32, &bound},
@@ -469,6 +636,8 @@ int main(int argc, char** argv) {
        &output},
       {"host-parse", 0, "parse the data file on the host instead of the GPU", wahcli::flag::BOOL,
        &host_parse},
+      {"device-merge", 0, "append the slices on the GPU and copy the merged index back once",
+       wahcli::flag::BOOL, &device_merge},
   };
   const int pf = wahcli::parse_flags(argc, argv, flags);
   if (pf != 0) return pf > 0 ? 0 : 2;
@@ -520,6 +689,15 @@ int main(int argc, char** argv) {
   const uint64_t slices = (std::max<uint64_t>(n, 1) + wg_size - 1) / wg_size;
   work_groups = static_cast<uint32_t>(std::min<uint64_t>(work_groups, slices));
 
+  // the column in page-locked memory: batches are copied to the device from it
+  wahcli::pinned_u32 column;
+  if (column.alloc(n) != WAH_OK) {
+    std::fprintf(stderr, "[!!!] %s\n", wah_strerror(WAH_ENOMEM));
+    return 1;
+  }
+  if (n) std::memcpy(column.p, values.data(), n * 4);
+  std::vector<uint32_t>().swap(values);
+
   int exit_code = 0;
   {
     actor_system system{4};
@@ -527,10 +705,18 @@ int main(int argc, char** argv) {
     actor w = system.spawn<worker_state>([](actor_ctx<worker_state>& self) { return worker(self); });
     actor x = system.spawn<indexer_state>(
         [](actor_ctx<indexer_state>& self) { return indexer(self); });
+    // the worker's buffers exist before the clock starts (the reference
+    // spawns its OpenCL worker before the indexer and merger, too)
+    int setup = WAH_OK;
+    {
+      scoped_actor self{system};
+      self.send(w, init_atom{}, dev, jobs, static_cast<uint32_t>(wg_size), work_groups, bound, x,
+                static_cast<const uint32_t*>(column.p), n, device_merge);
+      self.receive(handler<ready_atom, int>([&](ready_atom, int rc) { setup = rc; }));
+    }
+    if (setup != WAH_OK) std::fprintf(stderr, "[!!!] %s\n", wah_strerror(setup));
     system.send(m, init_atom{}, print_results, bound, output, &exit_code);
-    system.send(w, init_atom{}, dev, jobs, static_cast<uint32_t>(wg_size), work_groups, bound, x);
-    system.send(x, init_atom{}, w, m, std::move(values), jobs, work_groups,
-                static_cast<uint32_t>(wg_size));
+    system.send(x, init_atom{}, w, m, n, jobs, work_groups, static_cast<uint32_t>(wg_size));
     system.send(x, index_atom{});
     system.await_all_actors_done();
   }

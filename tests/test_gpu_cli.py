@@ -117,12 +117,14 @@ def test_gpu_builtin_fixture_listing(progs):
     assert listing(a.stdout) == listing(b.stdout)
 
 
+@pytest.mark.parametrize("merge", ["host", "device"])
 @pytest.mark.parametrize("batch,groups,jobs", [
     (1023, 1, 1), (1023, 1, 3), (31, 4, 2), (1023, 64, 2), (4096, 8, 3),
     (100_000, 1, 2), (65_534, 3, 4), (1 << 20, 1, 1)])
-def test_gpu_merged_index_matches_whole_column(progs, tmp_path, batch, groups, jobs):
+def test_gpu_merged_index_matches_whole_column(progs, tmp_path, batch, groups, jobs, merge):
     """Slices built separately (alone or many per batched launch) and merged
-    with re-based fills give the whole column's index (the reference's merger
+    with re-based fills -- on the host, or appended on the device
+    (--device-merge) -- give the whole column's index (the reference's merger
     does not)."""
     rng = np.random.default_rng(batch + groups + jobs)
     n = 200_003
@@ -131,7 +133,7 @@ def test_gpu_merged_index_matches_whole_column(progs, tmp_path, batch, groups, j
     data, out = tmp_path / "v.txt", tmp_path / "r.bin"
     write_values(data, v)
     r = run([progs["gpu"], "-f", str(data), "--batch-size", str(batch), "-w", str(groups),
-             "-j", str(jobs), "-o", str(out)])
+             "-j", str(jobs), "-o", str(out)] + (["--device-merge"] if merge == "device" else []))
     assert r.returncode == 0, r.stderr
     if batch % 31 and batch < n:
         assert "rounded to" in r.stdout
@@ -152,17 +154,27 @@ def test_gpu_sparse_keys_across_many_slices(progs, tmp_path):
     assert_matches_oracle(out, v, "gpu sparse")
 
 
-def test_gpu_single_value_and_empty(progs, tmp_path):
+@pytest.mark.parametrize("extra", [[], ["--device-merge"]])
+def test_gpu_single_value_and_empty(progs, tmp_path, extra):
     data, out = tmp_path / "v.txt", tmp_path / "r.bin"
     write_values(data, np.array([12345], np.uint32))
-    r = run([progs["gpu"], "-f", str(data), "-o", str(out)])
+    r = run([progs["gpu"], "-f", str(data), "-o", str(out)] + extra)
     assert r.returncode == 0, r.stderr
     assert_matches_oracle(out, np.array([12345], np.uint32), "gpu single")
     data.write_text("")
-    r = run([progs["gpu"], "-f", str(data), "-o", str(out)])
+    r = run([progs["gpu"], "-f", str(data), "-o", str(out)] + extra)
     assert r.returncode == 0, r.stderr
     keys, offsets, index = read_result(out)
     assert keys.size == 0 and index.size == 0
+
+
+def test_gpu_device_merge_listing_equals_cpu_program(progs, tmp_path):
+    """-p with --device-merge lists keys 0..bound from the merged index, as
+    the cpu program does."""
+    a = run([progs["gpu"], "-p", "--device-merge", "--batch-size", "31"])
+    b = run([progs["cpu"], "-p"])
+    assert a.returncode == 0, a.stderr
+    assert listing(a.stdout) == listing(b.stdout)
 
 
 def test_gpu_unknown_device_is_an_error(progs):
