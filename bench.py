@@ -4,7 +4,8 @@
 Default workload (one GPU): one column of 268,435,456 uint32 values, i.i.d.
 uniform in [0, 65535] from a seeded PRNG (numpy PCG64), bound = 65535 (the
 reference's -b).  A step is one full index build of that column: digit
-histogram, plan, two onesweep digit passes, fused index build.
+histogram, plan, two radix digit passes (per-range counts and scatter), fused
+index build.
 
 Printed: one JSON line on stdout.  Per-phase "N us" lines (the reference's
 SHOW_TIME_CONSUMPTION output, src/phases.cpp:714-1127) go to stderr.
@@ -23,6 +24,8 @@ SHOW_TIME_CONSUMPTION output, src/phases.cpp:714-1127) go to stderr.
               one-key / 1,000-key range queries
   ingest      the column as a one-value-per-line text file parsed on the
               device (resident text, and from pinned host memory)
+  c1          a 1,048,576-row column: device build latency and the build
+              through the host-buffer context API
   append      the index of the first ~3/4 of the column and the index of the
               rest appended on the device (wah_append), checked word for word
               against the whole-column build
@@ -76,13 +79,14 @@ def parse():
     ap.add_argument("--no-ingest", action="store_true")
     ap.add_argument("--no-decode", action="store_true")
     ap.add_argument("--no-append", action="store_true")
+    ap.add_argument("--no-c1", action="store_true")
     ap.add_argument("--serve-requests", type=int, default=20000)
     ap.add_argument("--serve-budget-gb", type=int, default=64)
     ap.add_argument("--pipe-depth", type=int, default=3,
                     help="builds in flight in the end-to-end leg")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--sort-items", type=int, default=0,
-                    help="onesweep rows per thread (0: library default)")
+                    help="radix scatter tuning: rows per thread | peer-mask flags (0: library default)")
     ap.add_argument("--cpu-sample", type=int, default=1 << 23,
                     help="rows per oracle build in the CPU legs")
     return ap.parse_args()
@@ -443,6 +447,46 @@ def bench_append(args, lib, wah, torch, dev, stream, d_values, n, bound, bufs, K
     return out
 
 
+def bench_c1(args, lib, wah, torch, dev, stream):
+    """The scope table's C1 column: 1,048,576 uint32 uniform [0, 65535]
+    (seeded).  Device-resident build latency (CUDA events over repeated
+    builds on the stream), and the same build through the host-buffer
+    context API (values in from page-locked host memory, keys, offsets and
+    index back to page-locked memory, wall clock per call)."""
+    n = 1 << 20
+    v = gen_uniform(n, 65536, args.seed + 1)
+    d_v = torch.from_numpy(v.view(np.int32)).to(dev)
+    b = wah._Buffers(n, 65535, dev)
+    sh = stream.cuda_stream
+
+    def build():
+        rc = lib.wah_build(d_v.data_ptr(), n, 65535, b.keys.data_ptr(), b.offsets.data_ptr(),
+                           b.index.data_ptr(), b.counts.data_ptr(), b.ws.data_ptr(), b.ws_bytes,
+                           sh)
+        assert rc == 0
+    for _ in range(5):
+        build()
+    reps = 200
+    ms = time_events(build, reps, torch, stream)
+    c = b.counts.cpu().numpy().view(np.uint32)
+    assert c[3] == 0
+    kc, ic = wah.output_caps(n, 65535)
+    pin = {name: torch.empty(size, dtype=torch.int32, pin_memory=True).numpy().view(np.uint32)
+           for name, size in (("v", n), ("k", kc), ("o", kc), ("i", ic))}
+    pin["v"][:] = v
+    with wah.HostContext(n, 65535) as ctx:
+        for _ in range(5):
+            ctx.build_into(pin["v"], pin["k"], pin["o"], pin["i"])
+        t0 = time.perf_counter()
+        for _ in range(50):
+            cnt = ctx.build_into(pin["v"], pin["k"], pin["o"], pin["i"])
+        host_ms = (time.perf_counter() - t0) * 1e3 / 50
+    assert int(cnt.keycnt) == int(c[0]) and int(cnt.index_len) == int(c[1])
+    return {"rows": n, "device_us": ms * 1e3, "device_rows_per_s": n / (ms / 1e3),
+            "host_api_us": host_ms * 1e3, "host_api_rows_per_s": n / (host_ms / 1e3),
+            "keycnt": int(c[0]), "index_len": int(c[1]), "merged": int(c[2])}
+
+
 def bench_serving(args, wah, torch, dev):
     """C5: Poisson arrivals of index-build requests (one pinned host column
     each), rows log-uniform in [10,000, 16,777,216], values uniform [0,65535],
@@ -711,6 +755,7 @@ def main():
     append = (None if args.no_append else
               bench_append(args, lib, wah, torch, dev, stream, d_values, n, bound, bufs, K, L))
     ingest = None if args.no_ingest else bench_ingest(args, lib, torch, dev, stream, d_values, n)
+    c1 = None if args.no_c1 else bench_c1(args, lib, wah, torch, dev, stream)
 
     # End to end: host values in, host index out, through the public
     # pipelined host-buffer API (wah_pipe_*): every step copies its column in
@@ -813,6 +858,7 @@ def main():
             "serving": serving,
             "decode": decode,
             "append": append,
+            "c1": c1,
             "ingest": ingest,
             "cpu_baseline": cpu,
         }

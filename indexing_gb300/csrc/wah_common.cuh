@@ -1,10 +1,11 @@
 // wah_common.cuh -- shared device helpers for the GB300 WAH index kernels.
 //
 // Layout of one build's device state (all in the caller's workspace):
-//   WahCtrl            digit histograms, per-pass bin offsets, pass plan,
-//                      dynamic tile counters
-//   sort look-back     one u32 per (tile, bin) for the onesweep passes
-//   build look-back    one u64 per tile for the fused index build
+//   WahCtrl            pass plan (trivial digits skipped, ping-pong homes),
+//                      OR of the keys and of their complements
+//   range arrays       per-(range, bin) digit counts and starts; per-range
+//                      word/key/segment counts and first positions of the
+//                      index build
 //   ping-pong buffers  sorted keys and row ids, 4 x n u32
 #pragma once
 
@@ -39,21 +40,6 @@ constexpr int kHistThreads = 256;
 constexpr int kHistUnroll = 4;  // uint4 loads in flight per thread
 constexpr int kHistWarps = kHistThreads / 32;
 
-// Look-back status in the top two bits of an entry.
-constexpr uint32_t kLbFlagShift32 = 30;
-constexpr uint32_t kLbAggregate32 = 1u << 30;
-constexpr uint32_t kLbPrefix32 = 2u << 30;
-constexpr uint32_t kLbMask32 = (1u << 30) - 1;
-constexpr uint64_t kLbAggregate64 = 1ull << 62;
-constexpr uint64_t kLbPrefix64 = 2ull << 62;
-constexpr uint64_t kLbMask64 = (1ull << 62) - 1;
-
-// Bounded waits: after kSpinFast polls a waiter sleeps between polls; after
-// kSpinLimit polls it gives up, records WAH_ETIMEOUT and carries on without
-// writing anything it could not place.
-constexpr uint32_t kSpinFast = 64;
-constexpr uint32_t kSpinLimit = 1u << 22;
-
 // Source/destination selectors of a sort pass.
 constexpr int kSelInput = 0;  // the caller's values, rid = row index
 constexpr int kSelA = 1;
@@ -63,7 +49,6 @@ struct WahCtrl {
   int32_t pass_src[kDigits];          // -1: pass skipped (trivial digit)
   int32_t pass_dst[kDigits];
   int32_t final_sel;                  // where the sorted stream ends up
-  uint32_t tile_ctr[8];               // [0..3] sort passes, [4] build
   uint32_t key_or;                    // OR of all keys (range check vs bound)
   uint32_t key_nor;                   // OR of the complements: bits some key has clear
   uint32_t pad[1];
