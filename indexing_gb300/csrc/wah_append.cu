@@ -17,12 +17,12 @@
 //            zero chunks before the key's first row in the slice) replaced by
 //            the zero chunks between A's last literal of the key and that
 //            row: fill = R/31 + lead - end_A, dropped when 0
-//   end_A    the chunk after a key's last literal in A: the walk over A's
-//            words (wah_walk.cuh) reports it for every key
+//   end_A    the chunk after a key's last literal in A: the sum of the
+//            chunk advances of the key's words (k_key_ends)
 //
 // Offsets are an exclusive scan of the per-key word counts; the words move
 // in load-balanced pieces of 4,096 (a scan over per-key piece counts tells
-// each CTA which key and part its piece belongs to).
+// each warp which key and part its pieces belong to).
 #include "wah_walk.cuh"
 
 namespace wah {
@@ -49,6 +49,23 @@ __device__ __forceinline__ uint32_t key_of_word(const uint32_t* offsets, uint32_
   return lo;
 }
 
+// First key of every tile of A's words: key k writes the tiles that start
+// inside its words (tile_key was zeroed; offsets are clamped so a corrupt
+// index cannot write out of range).
+__global__ void k_tile_keys(const uint32_t* __restrict__ offsets, uint32_t ka, uint32_t la,
+                            uint32_t* __restrict__ tile_key) {
+  const uint32_t ntiles = (uint32_t)ceil_div(la, kEndTile);
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < ka; k += gridDim.x * blockDim.x) {
+    uint32_t w1 = k + 1 < ka ? offsets[k + 1] : la;
+    w1 = w1 < la ? w1 : la;
+    uint32_t w0 = offsets[k];
+    w0 = w0 < w1 ? w0 : w1;
+    const uint32_t t_end = (uint32_t)ceil_div(w1, kEndTile);
+    for (uint32_t t = (uint32_t)ceil_div(w0, kEndTile); t < t_end && t < ntiles; ++t)
+      tile_key[t] = k;
+  }
+}
+
 // Tile word i lives at i + i/32 in shared memory: the coalesced loads
 // (consecutive i per warp) and the per-thread reads (i = 16 t + j) both
 // spread over all 32 banks.
@@ -57,25 +74,25 @@ __device__ __forceinline__ uint32_t end_skew(uint32_t i) { return i + (i >> 5); 
 __global__ void __launch_bounds__(256) k_key_ends(const uint32_t* __restrict__ offsets,
                                                   const uint32_t* __restrict__ index,
                                                   uint32_t ka, uint32_t la,
+                                                  const uint32_t* __restrict__ tile_key,
                                                   unsigned long long* __restrict__ ends) {
   __shared__ uint32_t s_w[kEndTile + kEndTile / 32];
-  __shared__ uint32_t s_span[2];
   const uint32_t ntiles = (uint32_t)ceil_div(la, kEndTile);
   const uint32_t lane = threadIdx.x & 31;
   for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
     const uint32_t t0 = t * kEndTile;
     const uint32_t t1 = la - t0 < kEndTile ? la : t0 + kEndTile;
-    if (threadIdx.x == 0) {
-      s_span[0] = key_of_word(offsets, 0, ka - 1, t0);
-      s_span[1] = key_of_word(offsets, 0, ka - 1, t1 - 1);
-    }
+    // the keys this tile touches: from its first word's key up to the next
+    // tile's first key (a bound on its last word's key)
+    const uint32_t k_lo = tile_key[t] < ka ? tile_key[t] : ka - 1;
+    const uint32_t k_nx = t + 1 < ntiles ? tile_key[t + 1] : ka - 1;
+    const uint32_t k_hi = k_nx < ka ? k_nx : ka - 1;
 #pragma unroll
     for (uint32_t j = 0; j < kEndItems; ++j) {
       const uint32_t i = j * 256 + threadIdx.x;
       s_w[end_skew(i)] = t0 + i < t1 ? index[t0 + i] : 0u;
     }
     __syncthreads();
-    const uint32_t k_lo = s_span[0], k_hi = s_span[1];
     const uint32_t l0 = threadIdx.x * kEndItems;  // this thread's first tile word
     uint32_t key = kNone;
     unsigned long long acc = 0;
@@ -101,7 +118,7 @@ __global__ void __launch_bounds__(256) k_key_ends(const uint32_t* __restrict__ o
     } else if (key != kNone) {
       atomicAdd(&ends[key], acc);
     }
-    __syncthreads();  // s_w and s_span are rewritten by the next tile
+    __syncthreads();  // s_w is rewritten by the next tile
   }
 }
 
@@ -283,36 +300,34 @@ __global__ void k_key_words(AppendIn in, const unsigned long long* ends, const u
   }
 }
 
-// Every piece: copy up to kPiece words of one key's A or B part.  Each CTA
+// Every piece: copy up to kPiece words of one key's A or B part.  Each warp
 // takes a contiguous share of the pieces: one binary search finds the key
 // of its first piece (the last key whose first piece is <= it), later pieces
-// step forward; each thread loads its 16 words of a piece before storing any.
-constexpr uint32_t kPieceItems = kPiece / kAThreads;
-static_assert(kPiece % kAThreads == 0, "whole items per thread");
+// step forward.  Warps work independently, so one warp's key lookups overlap
+// the others' copies; each lane keeps 8 loads in flight.
+constexpr uint32_t kCopyUnroll = 8;
 
 __global__ void __launch_bounds__(kAThreads) k_copy_pieces(
     AppendIn in, const unsigned long long* ends, const uint32_t* src_a, const uint32_t* src_b,
     const uint32_t* out_count, const uint32_t* piece_base, const uint32_t* total_pieces,
     const uint32_t* out_offsets, uint32_t* out_index, uint32_t* status) {
-  __shared__ uint32_t s_key;
   const uint32_t K = *out_count;
   const uint32_t T = *total_pieces;
-  const uint32_t per = (uint32_t)ceil_div(T, gridDim.x);
-  const uint64_t first = (uint64_t)blockIdx.x * per;
-  if (first >= T) return;  // no pieces left for this CTA
+  const uint32_t lane = threadIdx.x & 31;
+  const uint64_t warps = (uint64_t)gridDim.x * (kAThreads / 32);
+  const uint64_t wid = (uint64_t)blockIdx.x * (kAThreads / 32) + threadIdx.x / 32;
+  const uint64_t per = ceil_div(T, warps);
+  const uint64_t first = wid * per;
+  if (first >= T) return;  // no pieces left for this warp
   const uint32_t c0 = (uint32_t)first;
-  const uint32_t c1 = T - c0 < per ? T : c0 + per;
-  if (threadIdx.x == 0) {
-    uint32_t lo = 0, hi = K;
-    while (lo < hi) {
-      const uint32_t mid = (lo + hi) >> 1;
-      if (piece_base[mid] <= c0) lo = mid + 1;
-      else hi = mid;
-    }
-    s_key = lo - 1;
+  const uint32_t c1 = T - c0 < per ? T : c0 + (uint32_t)per;
+  uint32_t lo = 0, hi = K;  // every lane runs the same search (same loads)
+  while (lo < hi) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (piece_base[mid] <= c0) lo = mid + 1;
+    else hi = mid;
   }
-  __syncthreads();
-  uint32_t o = s_key;
+  uint32_t o = lo - 1;
   for (uint32_t c = c0; c < c1; ++c) {
     while (o + 1 < K && piece_base[o + 1] <= c) ++o;
     const KeyParts k = key_parts(in, ends, src_a[o], src_b[o], status);
@@ -333,16 +348,18 @@ __global__ void __launch_bounds__(kAThreads) k_copy_pieces(
       dst = out_index + dst0 + k.a_len + (k.gap ? 1u : 0u) + off;
       len = k.b_len - off < kPiece ? k.b_len - off : kPiece;
     }
-    uint32_t v[kPieceItems];
+    for (uint32_t base = 0; base < len; base += 32 * kCopyUnroll) {
+      uint32_t v[kCopyUnroll];
 #pragma unroll
-    for (uint32_t j = 0; j < kPieceItems; ++j) {
-      const uint32_t i = j * kAThreads + threadIdx.x;
-      if (i < len) v[j] = src[i];
-    }
+      for (uint32_t j = 0; j < kCopyUnroll; ++j) {
+        const uint32_t i = base + j * 32 + lane;
+        if (i < len) v[j] = src[i];
+      }
 #pragma unroll
-    for (uint32_t j = 0; j < kPieceItems; ++j) {
-      const uint32_t i = j * kAThreads + threadIdx.x;
-      if (i < len) dst[i] = v[j];
+      for (uint32_t j = 0; j < kCopyUnroll; ++j) {
+        const uint32_t i = base + j * 32 + lane;
+        if (i < len) dst[i] = v[j];
+      }
     }
   }
 }
@@ -451,10 +468,18 @@ int wah_append(const uint32_t* a_keys, const uint32_t* a_offsets, const uint32_t
   // 1. end chunk of every A key
   if (e == cudaSuccess && keycnt_a) e = cudaMemsetAsync(w.ends, 0, (size_t)keycnt_a * 8, s);
   if (e == cudaSuccess && keycnt_a && index_len_a) {
+    // each tile's first key, kept in the tail of out_index (its words are
+    // written only by the copy below, later on the same stream)
     const uint64_t tiles = ceil_div(index_len_a, kEndTile);
-    k_key_ends<<<(unsigned)std::min<uint64_t>(tiles, (uint64_t)grid * 2), 256, 0, s>>>(
-        a_offsets, a_index, keycnt_a, index_len_a, w.ends);
-    ++launches;
+    uint32_t* tile_key = out_index + (index_cap - tiles);
+    e = cudaMemsetAsync(tile_key, 0, tiles * 4, s);
+    if (e == cudaSuccess) {
+      k_tile_keys<<<(unsigned)std::min<uint64_t>(ceil_div(keycnt_a, 256), (uint64_t)grid), 256, 0,
+                    s>>>(a_offsets, keycnt_a, index_len_a, tile_key);
+      k_key_ends<<<(unsigned)std::min<uint64_t>(tiles, (uint64_t)grid * 2), 256, 0, s>>>(
+          a_offsets, a_index, keycnt_a, index_len_a, tile_key, w.ends);
+      launches += 2;
+    }
   }
   // 2. the merged key set: K = ka + B keys new to A
   if (e == cudaSuccess && kc) e = cudaMemsetAsync(w.src_a, 0xFF, kc * 4, s);
