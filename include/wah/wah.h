@@ -374,6 +374,9 @@ void wah_noop_graph_destroy(wah_noop_graph* graph);
  * chunks since the key's last row in A.  d_counts receives K, L and a
  * status (WAH_ECORRUPT when A has rows at or past rows_a).  All pointers are
  * device memory; workspace wah_append_workspace_bytes(keycnt_a, keycnt_b).
+ * out_index past the result's L words is scratch during the call (a table
+ * of index_len_a / 4,096 words sits at its end before the words are
+ * written).
  */
 size_t wah_append_workspace_bytes(uint32_t keycnt_a, uint32_t keycnt_b);
 int wah_append(const uint32_t* a_keys, const uint32_t* a_offsets,
