@@ -287,6 +287,14 @@ struct RangeView {
 __host__ __device__ __forceinline__ const uint32_t* sel_keys(const ColumnView& c, int s) {
   return s == kSelInput ? c.input : (s == kSelA ? c.keys_a : c.keys_b);
 }
+// A sort buffer between two digit passes holds 16-bit keys when every key
+// fits 16 bits (at most two digit passes, the bound checked by the sort
+// plan); the caller's input and the last pass's output (read by the index
+// build) keep 32-bit keys.  A narrow buffer uses the first half of its u32
+// array.  Valid once the sort plan has run.
+__device__ __forceinline__ bool narrow_keys(const ColumnView& c, int s) {
+  return c.passes <= 2 && s != kSelInput && s != c.ctrl->final_sel;
+}
 __host__ __device__ __forceinline__ const uint32_t* sel_rids(const ColumnView& c, int s) {
   return s == kSelInput ? c.input_rids : (s == kSelA ? c.rids_a : c.rids_b);
 }

@@ -93,11 +93,45 @@ __device__ __forceinline__ uint2 histogram_range(const uint32_t* __restrict__ ke
   return make_uint2(__reduce_or_sync(0xffffffffu, acc_or), __reduce_or_sync(0xffffffffu, acc_nor));
 }
 
+// 16-bit keys: the same over uint4 loads of 8 keys (lo a multiple of 8).
+template <int DIGITS>
+__device__ __forceinline__ void histogram_range16(const uint16_t* __restrict__ keys, uint64_t lo,
+                                                  uint64_t hi, int first,
+                                                  uint32_t (*s_h)[DIGITS][kRadix]) {
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t nwarps = blockDim.x >> 5;
+  WarpHist<DIGITS> wh{s_h[warp], first};
+  uint32_t acc_or = 0, acc_nor = 0;
+  const uint4* kv = reinterpret_cast<const uint4*>(keys + lo);
+  const uint64_t chunks = (hi - lo) / 256;  // 32 lanes x 8 keys
+  auto add8 = [&](const uint4& q) {
+    wh.add(q.x & 0xFFFFu, acc_or, acc_nor);
+    wh.add(q.x >> 16, acc_or, acc_nor);
+    wh.add(q.y & 0xFFFFu, acc_or, acc_nor);
+    wh.add(q.y >> 16, acc_or, acc_nor);
+    wh.add(q.z & 0xFFFFu, acc_or, acc_nor);
+    wh.add(q.z >> 16, acc_or, acc_nor);
+    wh.add(q.w & 0xFFFFu, acc_or, acc_nor);
+    wh.add(q.w >> 16, acc_or, acc_nor);
+  };
+  uint64_t c = warp;
+  for (; c + (kHistUnroll - 1) * nwarps < chunks; c += kHistUnroll * nwarps) {
+    uint4 q[kHistUnroll];
+#pragma unroll
+    for (int u = 0; u < kHistUnroll; ++u) q[u] = ld_stream_v4(kv + (c + u * nwarps) * 32 + lane);
+#pragma unroll
+    for (int u = 0; u < kHistUnroll; ++u) add8(q[u]);
+  }
+  for (; c < chunks; c += nwarps) add8(ld_stream_v4(kv + c * 32 + lane));
+  if (warp == 0)
+    for (uint64_t i = lo + chunks * 256 + lane; i < hi; i += 32) wh.add(keys[i], acc_or, acc_nor);
+}
+
 // Part q of a range: the rows one counting CTA covers (parts start on
-// multiples of 4 rows, so 16-byte loads stay aligned).
+// multiples of 8 rows, so 16-byte loads of 32- and 16-bit keys stay aligned).
 __device__ __forceinline__ void sub_range(const RangeView& rv, uint32_t q, uint64_t* lo,
                                           uint64_t* hi) {
-  const uint64_t part = ((rv.hi - rv.lo) / kCountCtasPerRange) & ~(uint64_t)3;
+  const uint64_t part = ((rv.hi - rv.lo) / kCountCtasPerRange) & ~(uint64_t)7;
   *lo = rv.lo + q * part;
   *hi = q + 1 == kCountCtasPerRange ? rv.hi : *lo + part;
 }
@@ -145,7 +179,10 @@ __global__ void __launch_bounds__(kHistThreads)
   __syncthreads();
   uint64_t lo, hi;
   sub_range(rv, blockIdx.x % kCountCtasPerRange, &lo, &hi);
-  histogram_range<1>(keys, lo, hi, pass, s_h);
+  if (narrow_keys(c, src))
+    histogram_range16<1>(reinterpret_cast<const uint16_t*>(keys), lo, hi, pass, s_h);
+  else
+    histogram_range<1>(keys, lo, hi, pass, s_h);
   __syncthreads();
   for (int j = threadIdx.x; j < kRadix; j += kHistThreads) {
     uint32_t s = 0;
@@ -296,15 +333,19 @@ __device__ __forceinline__ uint32_t digit_peers(uint32_t d) {
   }
 }
 
-// Issue the bulk copies of one whole tile (thread 0 only).
+// Issue the bulk copies of one whole tile (thread 0 only); k16: the keys are
+// 16-bit (tiles start on multiples of 8 rows, so the copy stays 16-byte aligned).
 __device__ __forceinline__ void fetch_tile(uint32_t* dst_k, uint32_t* dst_r, uint64_t* bar,
                                            const uint32_t* kin, const uint32_t* rin,
-                                           uint64_t base, uint32_t rows) {
-  const uint32_t bytes = rows * 4u;
+                                           uint64_t base, uint32_t rows, bool k16) {
+  const uint32_t kbytes = rows * (k16 ? 2u : 4u), rbytes = rows * 4u;
   fence_proxy_async_shared();
-  mbar_arrive_expect_tx(bar, rin ? 2 * bytes : bytes);
-  bulk_copy_g2s(dst_k, kin + base, bytes, bar);
-  if (rin) bulk_copy_g2s(dst_r, rin + base, bytes, bar);
+  mbar_arrive_expect_tx(bar, rin ? kbytes + rbytes : kbytes);
+  if (k16)
+    bulk_copy_g2s(dst_k, reinterpret_cast<const uint16_t*>(kin) + base, kbytes, bar);
+  else
+    bulk_copy_g2s(dst_k, kin + base, kbytes, bar);
+  if (rin) bulk_copy_g2s(dst_r, rin + base, rbytes, bar);
 }
 
 // PEERS: 0 all items by ballots, 1 all by match.any, 2 the first
@@ -334,6 +375,10 @@ __global__ void __launch_bounds__(kSortThreads, 2)
   uint32_t* __restrict__ kout = const_cast<uint32_t*>(sel_keys(col, dst));
   uint32_t* __restrict__ rout = const_cast<uint32_t*>(sel_rids(col, dst));
   uint32_t* status = col.status;
+  // 16-bit keys in the sort buffers (every key below 2^16)
+  const bool k16_in = narrow_keys(col, src), k16_out = narrow_keys(col, dst);
+  const uint16_t* kin16 = reinterpret_cast<const uint16_t*>(kin);
+  uint16_t* kout16 = reinterpret_cast<uint16_t*>(kout);
 
   const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const uint64_t lo = rv.lo, hi = rv.hi;
@@ -346,7 +391,8 @@ __global__ void __launch_bounds__(kSortThreads, 2)
     mbar_init(&sm.bar[1], 1);
     sm.abort = 0;
     fence_mbar_init();
-    if (hi - lo >= TILE) fetch_tile(sm.in_keys[0], sm.in_rids[0], &sm.bar[0], kin, rin, lo, TILE);
+    if (hi - lo >= TILE)
+      fetch_tile(sm.in_keys[0], sm.in_rids[0], &sm.bar[0], kin, rin, lo, TILE, k16_in);
   }
   __syncthreads();
 
@@ -365,7 +411,7 @@ __global__ void __launch_bounds__(kSortThreads, 2)
     // column's last tile can be ragged; it is read with plain loads instead.
     if (tid == 0 && i + 1 < ntiles && hi - (base + TILE) >= TILE)
       fetch_tile(sm.in_keys[cur ^ 1], sm.in_rids[cur ^ 1], &sm.bar[cur ^ 1], kin, rin,
-                 base + TILE, TILE);
+                 base + TILE, TILE, k16_in);
     // Zero the warp counters (the previous tile's last reads were fenced).
     {
       uint4* w4 = reinterpret_cast<uint4*>(&sm.whist[0][0][0]);
@@ -386,9 +432,15 @@ __global__ void __launch_bounds__(kSortThreads, 2)
     }
     __syncthreads();
     if (valid == TILE) {
-      const uint32_t* kp = sm.in_keys[cur] + row0;
+      if (k16_in) {
+        const uint16_t* kp = reinterpret_cast<const uint16_t*>(sm.in_keys[cur]) + row0;
 #pragma unroll
-      for (int j = 0; j < ITEMS; ++j) key[j] = kp[j * 32];
+        for (int j = 0; j < ITEMS; ++j) key[j] = kp[j * 32];
+      } else {
+        const uint32_t* kp = sm.in_keys[cur] + row0;
+#pragma unroll
+        for (int j = 0; j < ITEMS; ++j) key[j] = kp[j * 32];
+      }
     } else {
       // The column's ragged last tile: plain loads; rows past n get key
       // 0xFFFFFFFF (digit 255 in every pass: stable ranking puts them after
@@ -397,7 +449,7 @@ __global__ void __launch_bounds__(kSortThreads, 2)
 #pragma unroll
       for (int j = 0; j < ITEMS; ++j) {
         const uint32_t r = row0 + j * 32;
-        key[j] = r < valid ? kin[base + r] : 0xffffffffu;
+        key[j] = r < valid ? (k16_in ? kin16[base + r] : kin[base + r]) : 0xffffffffu;
         if (rin) sm.in_rids[cur][r] = r < valid ? rin[base + r] : 0u;
       }
     }
@@ -472,7 +524,8 @@ __global__ void __launch_bounds__(kSortThreads, 2)
           const uint32_t kk = out_keys[k];
           const uint32_t g = sm.bin_base[digit8(kk, pass)] + k;
           if (g < n32) {
-            kout[g] = kk;
+            if (k16_out) kout16[g] = (uint16_t)kk;
+            else kout[g] = kk;
             rout[g] = sm.out_rids[k];
           } else {
             set_status(status, WAH_ETIMEOUT);
@@ -603,10 +656,12 @@ __global__ void k_sort_deliver(ColumnView c, uint32_t* __restrict__ out_keys,
                                uint32_t* __restrict__ out_rids) {
   const int sel = c.ctrl->final_sel;
   const uint32_t* __restrict__ k = sel_keys(c, sel);
+  const uint16_t* __restrict__ k16 = reinterpret_cast<const uint16_t*>(k);
+  const bool narrow = narrow_keys(c, sel);
   const uint32_t* __restrict__ r = sel_rids(c, sel);
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < c.n; i += stride) {
-    out_keys[i] = k[i];
+    out_keys[i] = narrow ? k16[i] : k[i];
     out_rids[i] = r ? r[i] : (uint32_t)i;
   }
 }
