@@ -724,23 +724,33 @@ def main():
     ms_per_step = max_ms / args.steps
 
     # Algorithmic bytes per build: histogram 4n; digit pass 0 12n (read key,
-    # write key + rid), later passes 16n; build 8n + 4L + 8K (read sorted
-    # key + rid, write words, keys, offsets).  A phase (count + scan +
-    # kernel) and its main kernel are credited the same bytes; the roofline
-    # is taken on the longest single kernel.
+    # write key + rid), later passes 16n -- with two passes the key between
+    # them is 16-bit: pass 0 10n, pass 1 14n (2 + 4 in, 4 + 4 out); build
+    # 8n + 4L + 8K (read sorted key + rid, write words, keys, offsets).  A
+    # phase (count + scan + kernel) and its main kernel are credited the same
+    # bytes; the roofline is taken on the longest single kernel.
     passes = max(1, -(-(card - 1).bit_length() // 8))
+    mid16 = passes == 2
     alg = {"histogram": 4 * n, "plan": 0, "build": 8 * n + 4 * L + 8 * K}
     alg["emit"] = alg["build"]
     for p in range(4):
-        a = (12 * n if p == 0 else 16 * n) if p < passes else 0
+        if p >= passes:
+            a = 0
+        elif mid16:
+            a = 10 * n if p == 0 else 14 * n
+        else:
+            a = 12 * n if p == 0 else 16 * n
         alg[f"pass{p}"] = a
         alg[f"scatter{p}"] = a
     # DRAM bytes per row of each kernel (dram__bytes_read.sum +
     # dram__bytes_write.sum, one ncu capture of a 67,108,864-row uniform
     # 16-bit column with the same tile shape); traffic grows with rows.
-    traffic_per_row = {"histogram": 4.05, "scatter0": 15.11, "scatter1": 19.20, "emit": 15.32}
-    per_unit = {"histogram": "4 B/row", "scatter0": "12 B/row (key in, key + rid out)",
-                "scatter1": "16 B/row (key + rid in and out)",
+    traffic_per_row = {"histogram": 4.05, "scatter0": 13.03, "scatter1": 17.14, "emit": 15.32}
+    per_unit = {"histogram": "4 B/row",
+                "scatter0": ("10 B/row (key in, 16-bit key + rid out)" if mid16
+                             else "12 B/row (key in, key + rid out)"),
+                "scatter1": ("14 B/row (16-bit key + rid in, key + rid out)" if mid16
+                             else "16 B/row (key + rid in and out)"),
                 "emit": "8 B/row + 4 B/word + 8 B/key"}
     dom = max(KERNELS, key=lambda p: phase_ms[p])
     peak, peak_kind = load_peaks()
