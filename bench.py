@@ -726,18 +726,23 @@ def main():
     # Algorithmic bytes per build: histogram 4n; digit pass 0 12n (read key,
     # write key + rid), later passes 16n -- with two passes the key between
     # them is 16-bit: pass 0 10n, pass 1 14n (2 + 4 in, 4 + 4 out); build
-    # 8n + 4L + 8K (read sorted key + rid, write words, keys, offsets).  A
-    # phase (count + scan + kernel) and its main kernel are credited the same
+    # 8n + 4L + 8K (read sorted key + rid, write words, keys, offsets).  When
+    # both digits of a two-pass column vary, key-start bits (one per row)
+    # replace the sorted keys: pass 1 writes rids and the bits (10n + n/8)
+    # and the build reads rids and bits (4n + n/8 + 4L + 8K).  A phase
+    # (count + scan + kernel) and its main kernel are credited the same
     # bytes; the roofline is taken on the longest single kernel.
     passes = max(1, -(-(card - 1).bit_length() // 8))
     mid16 = passes == 2
-    alg = {"histogram": 4 * n, "plan": 0, "build": 8 * n + 4 * L + 8 * K}
+    derive = mid16 and card > 256
+    alg = {"histogram": 4 * n, "plan": 0,
+           "build": (4 * n + n // 8 if derive else 8 * n) + 4 * L + 8 * K}
     alg["emit"] = alg["build"]
     for p in range(4):
         if p >= passes:
             a = 0
         elif mid16:
-            a = 10 * n if p == 0 else 14 * n
+            a = 10 * n if p == 0 else (10 * n + n // 8 if derive else 14 * n)
         else:
             a = 12 * n if p == 0 else 16 * n
         alg[f"pass{p}"] = a
@@ -745,13 +750,16 @@ def main():
     # DRAM bytes per row of each kernel (dram__bytes_read.sum +
     # dram__bytes_write.sum, one ncu capture of a 67,108,864-row uniform
     # 16-bit column with the same tile shape); traffic grows with rows.
-    traffic_per_row = {"histogram": 4.05, "scatter0": 13.03, "scatter1": 17.14, "emit": 15.32}
+    traffic_per_row = {"histogram": 4.05, "scatter0": 13.05, "scatter1": 10.16, "emit": 11.29}
     per_unit = {"histogram": "4 B/row",
                 "scatter0": ("10 B/row (key in, 16-bit key + rid out)" if mid16
                              else "12 B/row (key in, key + rid out)"),
-                "scatter1": ("14 B/row (16-bit key + rid in, key + rid out)" if mid16
+                "scatter1": ("10 B/row + 1 bit (16-bit key + rid in, rid out, key-start bit)"
+                             if derive else
+                             "14 B/row (16-bit key + rid in, key + rid out)" if mid16
                              else "16 B/row (key + rid in and out)"),
-                "emit": "8 B/row + 4 B/word + 8 B/key"}
+                "emit": ("4 B/row + 1 bit + 4 B/word + 8 B/key" if derive
+                         else "8 B/row + 4 B/word + 8 B/key")}
     dom = max(KERNELS, key=lambda p: phase_ms[p])
     peak, peak_kind = load_peaks()
     ach = alg[dom] / (phase_ms[dom] / 1e3) / 1e9 if phase_ms[dom] > 0 else 0.0

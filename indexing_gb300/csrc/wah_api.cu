@@ -66,8 +66,8 @@ constexpr size_t kAlign = 256;
 inline size_t align_up(size_t x) { return (x + kAlign - 1) / kAlign * kAlign; }
 
 struct WsLayout {
-  size_t ctrl, range_hist, range_start, range_counts, range_first, keys_a, rids_a, keys_b,
-      rids_b, total;
+  size_t ctrl, range_hist, range_start, range_counts, range_first, keyhist, keystart, keys_a,
+      rids_a, keys_b, rids_b, total;
 };
 
 WsLayout ws_layout(uint64_t n) {
@@ -83,6 +83,10 @@ WsLayout ws_layout(uint64_t n) {
   off += align_up((size_t)kMaxRanges * 4 * sizeof(uint32_t));
   l.range_first = off;
   off += align_up((size_t)kMaxRanges * 2 * sizeof(uint32_t));
+  l.keyhist = off;
+  off += align_up((size_t)65536 * sizeof(uint32_t));
+  l.keystart = off;
+  off += align_up((ceil_div(std::max<uint64_t>(n, 1), 32) + 16) * sizeof(uint32_t));
   const size_t col = align_up(std::max<uint64_t>(n, 1) * sizeof(uint32_t));
   l.keys_a = off;
   off += col;
@@ -109,6 +113,9 @@ void workspace_views(const WsLayout& l, unsigned char* ws, uint64_t n, ColumnVie
   c->keys_b = reinterpret_cast<uint32_t*>(ws + l.keys_b);
   c->rids_b = reinterpret_cast<uint32_t*>(ws + l.rids_b);
   c->fixed_sel = -1;
+  c->keyhist = reinterpret_cast<uint32_t*>(ws + l.keyhist);
+  c->keystart = reinterpret_cast<uint32_t*>(ws + l.keystart);
+  c->derive_ok = 0;
   ra->hist = reinterpret_cast<uint32_t*>(ws + l.range_hist);
   ra->start = reinterpret_cast<uint32_t*>(ws + l.range_start);
   ra->counts = reinterpret_cast<uint32_t*>(ws + l.range_counts);
@@ -186,6 +193,7 @@ static int build_impl(const uint32_t* d_values, uint64_t n, uint32_t bound, uint
   c.counts = d_counts;
   c.status = &d_counts->status;
   c.passes = passes_for_bound(bound);
+  c.derive_ok = 1;  // an index build: the sorted keys themselves are never read back
   const LaunchOpts o = launch_opts(c.passes, events);
   if (o.sm_count <= 0) return WAH_ENODEV;
   e = cudaMemsetAsync(c.ctrl, 0, sizeof(WahCtrl), s);

@@ -49,6 +49,7 @@ struct WahCtrl {
   int32_t pass_src[kDigits];          // -1: pass skipped (trivial digit)
   int32_t pass_dst[kDigits];
   int32_t final_sel;                  // where the sorted stream ends up
+  int32_t derive;                     // key starts replace the sorted keys (ColumnView)
   uint32_t key_or;                    // OR of all keys (range check vs bound)
   uint32_t key_nor;                   // OR of the complements: bits some key has clear
   uint32_t pad[1];
@@ -276,6 +277,15 @@ struct ColumnView {
   uint32_t* status;    // device-side errors of this column
   int32_t passes;      // digit passes its bound allows (1..4)
   int32_t fixed_sel;   // >= 0: the build reads this home instead of final_sel
+  // Key starts instead of sorted keys (two active digit passes, index builds
+  // of one column): the pass-1 count also counts every 16-bit key
+  // (keyhist[65536]), k_key_starts marks where each key starts in the sorted
+  // order (keystart, one bit per row) and writes the keys; the last pass then
+  // writes row ids only and the index build reads the bits instead of keys.
+  uint32_t* keyhist;
+  uint32_t* keystart;
+  int32_t derive_ok;
+  int32_t pad2;
 };
 
 struct RangeView {

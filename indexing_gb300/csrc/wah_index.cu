@@ -31,6 +31,7 @@
 //                  running offsets.  No zero word is ever written and no
 //                  compaction pass is needed.
 #include <algorithm>
+#include <type_traits>
 
 #include "wah_common.cuh"
 
@@ -57,6 +58,16 @@ constexpr uint64_t kPackMask = (1ull << kPackShift) - 1;
 // ---------------------------------------------------------------------------
 // Count: words, keys, segments per range.
 // ---------------------------------------------------------------------------
+// vh: the row starts a key (derive mode reads it from the key-start bits)
+__device__ __forceinline__ void count_row_h(bool vh, uint32_t c, uint32_t pc, uint32_t& words,
+                                            uint32_t& keys, uint32_t& segs) {
+  const bool h = vh || c != pc;
+  const uint32_t fill = vh ? c : c - pc - 1;
+  words += h ? 1u + (fill != 0) : 0u;
+  keys += vh;
+  segs += h;
+}
+
 __device__ __forceinline__ void count_row(uint32_t v, uint32_t c, uint32_t pv, uint32_t pc,
                                           uint32_t& words, uint32_t& keys, uint32_t& segs) {
   const bool vh = v != pv;
@@ -84,6 +95,47 @@ __global__ void __launch_bounds__(kHistThreads)
 
   uint32_t words = 0, keys = 0, segs = 0;
   const uint64_t chunks = (hi - lo) / 128;  // 32 lanes x 4 rows
+  if (col.fixed_sel < 0 && col.ctrl->derive) {
+    // key heads from the key-start bits (rows p..p+3 share one bit word),
+    // chunks from the row ids; no keys read
+    const uint32_t* __restrict__ ks = col.keystart;
+    // loads of kHistUnroll chunks issued together, then counted
+    auto count4 = [&](const uint4& r4, uint32_t bits, uint32_t pr) {
+      const uint32_t up = __shfl_up_sync(0xffffffffu, r4.w, 1);
+      const uint32_t pc = (lane == 0 ? pr : up) / 31;
+      const uint32_t c0 = r4.x / 31, c1 = r4.y / 31, c2 = r4.z / 31, c3 = r4.w / 31;
+      count_row_h(bits & 1u, c0, pc, words, keys, segs);
+      count_row_h((bits >> 1) & 1u, c1, c0, words, keys, segs);
+      count_row_h((bits >> 2) & 1u, c2, c1, words, keys, segs);
+      count_row_h((bits >> 3) & 1u, c3, c2, words, keys, segs);
+    };
+    uint64_t k = warp;
+    for (; k + (kHistUnroll - 1) * kHistWarps < chunks; k += kHistUnroll * kHistWarps) {
+      uint4 r4[kHistUnroll];
+      uint32_t bits[kHistUnroll], pr[kHistUnroll];
+#pragma unroll
+      for (int u = 0; u < kHistUnroll; ++u) {
+        const uint64_t p = lo + (k + u * kHistWarps) * 128 + lane * 4;
+        r4[u] = ld_stream_v4(reinterpret_cast<const uint4*>(sr + p));
+        bits[u] = ks[p >> 5] >> (p & 31);
+        pr[u] = (lane == 0 && p > 0) ? sr[p - 1] : 0u;
+      }
+#pragma unroll
+      for (int u = 0; u < kHistUnroll; ++u) count4(r4[u], bits[u], pr[u]);
+    }
+    for (; k < chunks; k += kHistWarps) {
+      const uint64_t p = lo + k * 128 + lane * 4;
+      const uint4 r4 = ld_stream_v4(reinterpret_cast<const uint4*>(sr + p));
+      count4(r4, ks[p >> 5] >> (p & 31), (lane == 0 && p > 0) ? sr[p - 1] : 0u);
+    }
+    if (warp == 0) {
+      for (uint64_t p = lo + chunks * 128 + lane; p < hi; p += 32) {
+        const uint32_t cc = sr[p] / 31;
+        const uint32_t pc = p > 0 ? sr[p - 1] / 31 : 0u;
+        count_row_h((ks[p >> 5] >> (p & 31)) & 1u, cc, pc, words, keys, segs);
+      }
+    }
+  } else {
   for (uint64_t k = warp; k < chunks; k += kHistWarps) {
     const uint64_t p = lo + k * 128 + lane * 4;
     const uint4 v4 = ld_stream_v4(reinterpret_cast<const uint4*>(sv + p));
@@ -126,6 +178,7 @@ __global__ void __launch_bounds__(kHistThreads)
       }
       count_row(v, cc, pv, pc, words, keys, segs);
     }
+  }
   }
 #pragma unroll
   for (int d = 16; d > 0; d >>= 1) {
@@ -192,21 +245,28 @@ __device__ __forceinline__ bool window_bulk(uint64_t base, uint64_t n) {
   return base >= (uint64_t)kWinBehind && base + kBuildTile + 32 <= n;
 }
 
+// Derive mode: the key-start bits of rows base .. base+TILE+95 take the
+// place of the keys in wv (base is a multiple of the tile, so the bit words
+// start 16-byte aligned; the bit array has 16 words of slack at its end).
+constexpr uint32_t kWinBitWords = 68;
+
 __device__ __forceinline__ void fetch_window(uint32_t* wv, uint32_t* wr, uint64_t* bar,
                                              const uint32_t* sv, const uint32_t* sr,
-                                             uint64_t base) {
+                                             const uint32_t* ks, uint64_t base, bool derive) {
   const uint32_t bytes = kWinRows * 4u;
+  const uint32_t vbytes = derive ? kWinBitWords * 4u : bytes;
   fence_proxy_async_shared();
-  mbar_arrive_expect_tx(bar, sr ? 2 * bytes : bytes);
-  bulk_copy_g2s(wv, sv + base - kWinBehind, bytes, bar);
+  mbar_arrive_expect_tx(bar, vbytes + (sr ? bytes : 0u));
+  if (derive) bulk_copy_g2s(wv, ks + (base >> 5), vbytes, bar);
+  else bulk_copy_g2s(wv, sv + base - kWinBehind, bytes, bar);
   if (sr) bulk_copy_g2s(wr, sr + base - kWinBehind, bytes, bar);
 }
 
-template <class G>
-__global__ void __launch_bounds__(kBuildThreads, 3)
-    k_build_emit(G g, const uint32_t* __restrict__ range_first) {
-  extern __shared__ __align__(128) unsigned char smem_raw[];
-  EmitSmem& sm = *reinterpret_cast<EmitSmem*>(smem_raw);
+// kDerive: key heads from the key-start bits, keys written already (derive
+// mode, one column only)
+template <class G, bool kDerive>
+__device__ __forceinline__ void build_emit(const G& g, const uint32_t* __restrict__ range_first,
+                                           EmitSmem& sm) {
   const RangeView rv = g.range(blockIdx.x);
   const ColumnView col = g.col(rv.col);
   const int s = col.fixed_sel >= 0 ? col.fixed_sel : col.ctrl->final_sel;
@@ -217,6 +277,8 @@ __global__ void __launch_bounds__(kBuildThreads, 3)
   uint32_t* __restrict__ out_offsets = col.offsets;
   const uint64_t keys_cap = col.keys_cap, index_cap = col.index_cap;
   uint32_t* status = col.status;
+  constexpr bool derive = kDerive;
+  const uint32_t* __restrict__ ks = col.keystart;
 
   const uint32_t tid = threadIdx.x;
   const uint64_t n = col.n;
@@ -231,7 +293,8 @@ __global__ void __launch_bounds__(kBuildThreads, 3)
     mbar_init(&sm.bar[1], 1);
     sm.abort = 0;
     fence_mbar_init();
-    if (window_bulk(lo, n)) fetch_window(sm.win_v[0], sm.win_r[0], &sm.bar[0], sv, sr, lo);
+    if (window_bulk(lo, n))
+      fetch_window(sm.win_v[0], sm.win_r[0], &sm.bar[0], sv, sr, ks, lo, derive);
   }
   __syncthreads();
 
@@ -242,8 +305,8 @@ __global__ void __launch_bounds__(kBuildThreads, 3)
     const uint64_t base = lo + (uint64_t)i * kBuildTile;
     const uint32_t valid = hi - base < kBuildTile ? (uint32_t)(hi - base) : kBuildTile;
     if (tid == 0 && i + 1 < ntiles && window_bulk(base + kBuildTile, n))
-      fetch_window(sm.win_v[cur ^ 1], sm.win_r[cur ^ 1], &sm.bar[cur ^ 1], sv, sr,
-                   base + kBuildTile);
+      fetch_window(sm.win_v[cur ^ 1], sm.win_r[cur ^ 1], &sm.bar[cur ^ 1], sv, sr, ks,
+                   base + kBuildTile, derive);
     uint32_t* wv = sm.win_v[cur];
     uint32_t* wr = sm.win_r[cur];
     // rows of the window that exist, counted from the tile start
@@ -270,21 +333,28 @@ __global__ void __launch_bounds__(kBuildThreads, 3)
       for (uint32_t w = tid; w < kWinRows; w += kBuildThreads) {
         const uint64_t row = base - kWinBehind + w;  // wraps below row 0: excluded
         if (row < n) {
-          wv[w] = sv[row];
+          if (!derive) wv[w] = sv[row];
           wr[w] = sr ? sr[row] : (uint32_t)row;
         }
       }
+      if (derive && tid < kWinBitWords && base + 32ull * tid < n) wv[tid] = ks[(base >> 5) + tid];
       __syncthreads();
     }
 
     // This thread's 8 rows from the window (two 16-byte loads per array).
     uint32_t v[kBuildItems], cb[kBuildItems];
     {
-      const uint4* v4 = reinterpret_cast<const uint4*>(wv + kWinBehind + first);
       const uint4* r4 = reinterpret_cast<const uint4*>(wr + kWinBehind + first);
-      const uint4 a0 = v4[0], a1 = v4[1], b0 = r4[0], b1 = r4[1];
-      v[0] = a0.x; v[1] = a0.y; v[2] = a0.z; v[3] = a0.w;
-      v[4] = a1.x; v[5] = a1.y; v[6] = a1.z; v[7] = a1.w;
+      const uint4 b0 = r4[0], b1 = r4[1];
+      if (!derive) {
+        const uint4* v4 = reinterpret_cast<const uint4*>(wv + kWinBehind + first);
+        const uint4 a0 = v4[0], a1 = v4[1];
+        v[0] = a0.x; v[1] = a0.y; v[2] = a0.z; v[3] = a0.w;
+        v[4] = a1.x; v[5] = a1.y; v[6] = a1.z; v[7] = a1.w;
+      } else {
+#pragma unroll
+        for (int j = 0; j < kBuildItems; ++j) v[j] = 0;
+      }
       cb[0] = chunk_bit(b0.x); cb[1] = chunk_bit(b0.y); cb[2] = chunk_bit(b0.z);
       cb[3] = chunk_bit(b0.w); cb[4] = chunk_bit(b1.x); cb[5] = chunk_bit(b1.y);
       cb[6] = chunk_bit(b1.z); cb[7] = chunk_bit(b1.w);
@@ -296,12 +366,15 @@ __global__ void __launch_bounds__(kBuildThreads, 3)
     // the row before the thread's first row (row 0 of the column heads a key)
     uint32_t pv, pc;
     if (base + first > 0) {
-      pv = wv[kWinBehind + first - 1];
+      pv = derive ? 0u : wv[kWinBehind + first - 1];
       pc = wr[kWinBehind + first - 1] / 31;
     } else {
       pv = ~v[0];
       pc = 0;
     }
+    // derive mode: which of this thread's 8 rows start a key (one bit word;
+    // the row offset is a multiple of 8)
+    const uint32_t kbits = derive ? (wv[first >> 5] >> (first & 31)) & 0xFFu : 0u;
 
     uint32_t headm = 0, vheadm = 0, fills[kBuildItems];
     uint32_t nw = 0;
@@ -309,7 +382,7 @@ __global__ void __launch_bounds__(kBuildThreads, 3)
     for (int j = 0; j < kBuildItems; ++j) {
       const uint32_t c = cb[j] >> 5;
       const bool ok = full || first + j < valid;
-      const bool vh = v[j] != pv;
+      const bool vh = derive ? ((kbits >> j) & 1u) != 0 : v[j] != pv;
       const bool h = ok && (vh || c != pc);
       fills[j] = vh ? c : c - pc - 1;
       if (h) {
@@ -329,7 +402,12 @@ __global__ void __launch_bounds__(kBuildThreads, 3)
       const uint32_t v7 = v[kBuildItems - 1], c7 = cb[kBuildItems - 1] >> 5;
       for (uint32_t m = first + kBuildItems; m < wend; ++m) {
         const uint32_t rm = wr[kWinBehind + m];
-        if (wv[kWinBehind + m] != v7 || rm / 31 != c7) break;
+        if (rm / 31 != c7) break;
+        if (derive) {
+          if ((wv[m >> 5] >> (m & 31)) & 1u) break;  // m < wend <= TILE + 30
+        } else if (wv[kWinBehind + m] != v7) {
+          break;
+        }
         acc |= 1u << (rm % 31);
       }
     }
@@ -353,7 +431,7 @@ __global__ void __launch_bounds__(kBuildThreads, 3)
     for (int j = 0; j < kBuildItems; ++j) {
       if (headm & (1u << j)) {
         if (vheadm & (1u << j)) {
-          sm.keys[skew(pk)] = v[j];
+          if (!derive) sm.keys[skew(pk)] = v[j];
           sm.offs[skew(pk)] = run_w + pw;
           ++pk;
         }
@@ -395,7 +473,7 @@ __global__ void __launch_bounds__(kBuildThreads, 3)
       for (uint32_t k = tid; k < tk; k += kBuildThreads) {
         const uint64_t pos = (uint64_t)run_k + k;
         if (pos < keys_cap) {
-          out_keys[pos] = sm.keys[skew(k)];
+          if (!derive) out_keys[pos] = sm.keys[skew(k)];
           out_offsets[pos] = sm.offs[skew(k)];
         } else {
           overflow = true;
@@ -407,6 +485,21 @@ __global__ void __launch_bounds__(kBuildThreads, 3)
     run_k += tk;
     __syncthreads();  // staging and window buffer reusable
   }
+}
+
+template <class G>
+__global__ void __launch_bounds__(kBuildThreads, 3)
+    k_build_emit(G g, const uint32_t* __restrict__ range_first) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  EmitSmem& sm = *reinterpret_cast<EmitSmem*>(smem_raw);
+  if constexpr (std::is_same<G, OneColumn>::value) {
+    const ColumnView& col = g.col(0);
+    if (col.fixed_sel < 0 && col.ctrl->derive) {
+      build_emit<G, true>(g, range_first, sm);
+      return;
+    }
+  }
+  build_emit<G, false>(g, range_first, sm);
 }
 
 // ---------------------------------------------------------------------------

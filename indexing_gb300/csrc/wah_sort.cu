@@ -26,6 +26,7 @@
 //                      out run by run at the range's running bin offsets.  The
 //                      first active pass takes rid = row index.
 #include <algorithm>
+#include <type_traits>
 
 #include "wah_common.cuh"
 
@@ -127,6 +128,80 @@ __device__ __forceinline__ void histogram_range16(const uint16_t* __restrict__ k
     for (uint64_t i = lo + chunks * 256 + lane; i < hi; i += 32) wh.add(keys[i], acc_or, acc_nor);
 }
 
+// 16-bit keys in order of their low digit (the pass-0 output): the digit-1
+// counts of the range as histogram_range16 gives them, and every full key
+// counted into keyhist.  A 256-row chunk whose first and last keys share the
+// low digit (all but at most 255 chunks of the column: each low digit's rows
+// are contiguous) counts its keys' high digits into the warp's counters for
+// that low digit, hw, which go to the range's digit-1 counts h1 and to
+// keyhist when the warp's low digit changes (one shared atomic per key, as
+// in histogram_range16); a chunk that spans low digits adds its keys to h1
+// and keyhist one by one.
+__device__ __forceinline__ void flush_keyhist(uint32_t* hw, uint32_t* h1, uint32_t d0,
+                                              uint32_t lane, uint32_t* __restrict__ keyhist) {
+  __syncwarp();
+  for (uint32_t d1 = lane; d1 < kRadix; d1 += 32) {
+    const uint32_t x = hw[d1];
+    if (x) {
+      h1[d1] += x;  // the warp's own counters, one lane per bin
+      atomicAdd(&keyhist[(d1 << 8) | d0], x);
+      hw[d1] = 0;
+    }
+  }
+  __syncwarp();
+}
+
+__device__ __forceinline__ void histogram_range16_full(const uint16_t* __restrict__ keys,
+                                                       uint64_t lo, uint64_t hi,
+                                                       uint32_t (*s_h)[1][kRadix],
+                                                       uint32_t (*s_full)[kRadix],
+                                                       uint32_t* __restrict__ keyhist) {
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t nwarps = blockDim.x >> 5;
+  uint32_t* h1 = s_h[warp][0];    // digit-1 counts of the range
+  uint32_t* hw = s_full[warp];    // digit-1 counts for the warp's current low digit
+  uint32_t cur = kRadix;          // the low digit hw counts (none yet)
+  const uint4* kv = reinterpret_cast<const uint4*>(keys + lo);
+  const uint64_t chunks = (hi - lo) / 256;  // 32 lanes x 8 keys
+  auto add_chunk = [&](const uint4& q) {
+    const uint32_t k8[8] = {q.x & 0xFFFFu, q.x >> 16, q.y & 0xFFFFu, q.y >> 16,
+                            q.z & 0xFFFFu, q.z >> 16, q.w & 0xFFFFu, q.w >> 16};
+    const uint32_t first = __shfl_sync(0xffffffffu, k8[0], 0) & 0xFFu;
+    const uint32_t last = __shfl_sync(0xffffffffu, k8[7], 31) & 0xFFu;
+    if (first == last) {
+      if (first != cur) {
+        if (cur < kRadix) flush_keyhist(hw, h1, cur, lane, keyhist);
+        cur = first;
+      }
+#pragma unroll
+      for (int i = 0; i < 8; ++i) atomicAdd(&hw[k8[i] >> 8], 1u);
+    } else {
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        atomicAdd(&h1[k8[i] >> 8], 1u);
+        atomicAdd(&keyhist[k8[i]], 1u);
+      }
+    }
+  };
+  uint64_t c = warp;
+  for (; c + (kHistUnroll - 1) * nwarps < chunks; c += kHistUnroll * nwarps) {
+    uint4 q[kHistUnroll];
+#pragma unroll
+    for (int u = 0; u < kHistUnroll; ++u) q[u] = ld_stream_v4(kv + (c + u * nwarps) * 32 + lane);
+#pragma unroll
+    for (int u = 0; u < kHistUnroll; ++u) add_chunk(q[u]);
+  }
+  for (; c < chunks; c += nwarps) add_chunk(ld_stream_v4(kv + c * 32 + lane));
+  if (cur < kRadix) flush_keyhist(hw, h1, cur, lane, keyhist);
+  __syncwarp();
+  if (warp == 0)
+    for (uint64_t i = lo + chunks * 256 + lane; i < hi; i += 32) {
+      const uint32_t k = keys[i];
+      atomicAdd(&h1[k >> 8], 1u);
+      atomicAdd(&keyhist[k], 1u);
+    }
+}
+
 // Part q of a range: the rows one counting CTA covers (parts start on
 // multiples of 8 rows, so 16-byte loads of 32- and 16-bit keys stay aligned).
 __device__ __forceinline__ void sub_range(const RangeView& rv, uint32_t q, uint64_t* lo,
@@ -175,11 +250,18 @@ __global__ void __launch_bounds__(kHistThreads)
   if (src < 0) return;
   const uint32_t* keys = sel_keys(c, src);
   __shared__ uint32_t s_h[kHistWarps][1][kRadix];
-  for (int i = threadIdx.x; i < kHistWarps * kRadix; i += kHistThreads) (&s_h[0][0][0])[i] = 0;
+  __shared__ uint32_t s_full[kHistWarps][kRadix];
+  for (int i = threadIdx.x; i < kHistWarps * kRadix; i += kHistThreads) {
+    (&s_h[0][0][0])[i] = 0;
+    (&s_full[0][0])[i] = 0;
+  }
   __syncthreads();
   uint64_t lo, hi;
   sub_range(rv, blockIdx.x % kCountCtasPerRange, &lo, &hi);
-  if (narrow_keys(c, src))
+  if (c.ctrl->derive && pass == 1)  // 16-bit keys in low-digit order
+    histogram_range16_full(reinterpret_cast<const uint16_t*>(keys), lo, hi, s_h, s_full,
+                           c.keyhist);
+  else if (narrow_keys(c, src))
     histogram_range16<1>(reinterpret_cast<const uint16_t*>(keys), lo, hi, pass, s_h);
   else
     histogram_range<1>(keys, lo, hi, pass, s_h);
@@ -206,6 +288,7 @@ __global__ void __launch_bounds__(kRadix) k_sort_plan(G g) {
     const uint32_t varying = ctrl->key_or & ctrl->key_nor;
     int s_active[kDigits];
     for (int p = 0; p < kDigits; ++p) s_active[p] = digit8(varying, p) != 0;
+    ctrl->derive = c.derive_ok && passes == 2 && s_active[0] && s_active[1];
     // A set bit above the digits the bound allows: the sort would be wrong.
     if (passes < kDigits && (ctrl->key_or >> (passes * kRadixBits)) != 0)
       set_status(status, WAH_ERANGE);
@@ -223,6 +306,44 @@ __global__ void __launch_bounds__(kRadix) k_sort_plan(G g) {
     }
     ctrl->final_sel = cur;
   }
+}
+
+// Key starts (derive mode): keyhist scanned in key order; the first row of
+// every present key in the sorted order gets its bit in keystart, and the
+// keys go to the output in order (the index build writes their offsets).
+// One thread per key; each CTA first sums the rows and present keys below
+// its own 1024 keys.  Rows (< 2^32) and present keys pack into one 64-bit sum.
+constexpr int kKeyStartThreads = 1024;
+constexpr int kKeyStartCtas = 65536 / kKeyStartThreads;
+
+template <class G>
+__global__ void __launch_bounds__(kKeyStartThreads) k_key_starts(G g) {
+  __shared__ uint64_t s_warp[kKeyStartThreads / 32 + 1];
+  const ColumnView c = g.col(0);
+  if (!c.ctrl->derive) return;
+  const uint32_t k0 = blockIdx.x * kKeyStartThreads;
+  const uint4* kh4 = reinterpret_cast<const uint4*>(c.keyhist);
+  uint64_t below = 0;
+#pragma unroll 4
+  for (uint32_t k = threadIdx.x; k < k0 / 4; k += kKeyStartThreads) {
+    const uint4 h = kh4[k];
+    const uint32_t present = (h.x != 0) + (h.y != 0) + (h.z != 0) + (h.w != 0);
+    below += (uint64_t)(h.x + h.y + h.z + h.w) | ((uint64_t)present << 32);
+  }
+  uint64_t base;
+  block_exclusive_scan64<kKeyStartThreads>(below, &base, s_warp);
+  const uint32_t key = k0 + threadIdx.x;
+  const uint32_t h = c.keyhist[key];
+  uint64_t total;
+  const uint64_t pre =
+      base + block_exclusive_scan64<kKeyStartThreads>(
+                 (uint64_t)h | ((uint64_t)(h != 0) << 32), &total, s_warp);
+  if (!h) return;
+  const uint32_t row = (uint32_t)pre, rank = (uint32_t)(pre >> 32);
+  if (row < c.n) atomicOr(&c.keystart[row >> 5], 1u << (row & 31));
+  else set_status(c.status, WAH_ECORRUPT);
+  if (rank < c.keys_cap) c.keys[rank] = key;
+  else set_status(c.status, WAH_EOVERFLOW);
 }
 
 // Start of every (range, bin) of one column for one pass: the bin's offset
@@ -377,6 +498,8 @@ __global__ void __launch_bounds__(kSortThreads, 2)
   uint32_t* status = col.status;
   // 16-bit keys in the sort buffers (every key below 2^16)
   const bool k16_in = narrow_keys(col, src), k16_out = narrow_keys(col, dst);
+  // derive mode: the last pass writes row ids only
+  const bool keys_out = !(col.ctrl->derive && dst == col.ctrl->final_sel);
   const uint16_t* kin16 = reinterpret_cast<const uint16_t*>(kin);
   uint16_t* kout16 = reinterpret_cast<uint16_t*>(kout);
 
@@ -524,8 +647,10 @@ __global__ void __launch_bounds__(kSortThreads, 2)
           const uint32_t kk = out_keys[k];
           const uint32_t g = sm.bin_base[digit8(kk, pass)] + k;
           if (g < n32) {
-            if (k16_out) kout16[g] = (uint16_t)kk;
-            else kout[g] = kk;
+            if (keys_out) {
+              if (k16_out) kout16[g] = (uint16_t)kk;
+              else kout[g] = kk;
+            }
             rout[g] = sm.out_rids[k];
           } else {
             set_status(status, WAH_ETIMEOUT);
@@ -608,6 +733,12 @@ cudaError_t launch_sort_t(const G& g, uint32_t ncols, uint32_t ranges, const Ran
       k_range_count<G><<<count_grid, kHistThreads, 0, s>>>(g, p, rh);
       ++*launches;
     }
+    if constexpr (std::is_same<G, OneColumn>::value) {
+      if (p == 1 && g.c.derive_ok && g.c.passes == 2) {  // works only in derive mode
+        k_key_starts<G><<<kKeyStartCtas, kKeyStartThreads, 0, s>>>(g);
+        ++*launches;
+      }
+    }
     k_range_scan<G><<<ncols, kRangeScanThreads, 0, s>>>(g, p, rh, ra.start);
     ++*launches;
     record_phase(o.events, kPhaseScatter0 + p, false, s);
@@ -633,6 +764,11 @@ cudaError_t launch_sort_one(const ColumnView& c, const RangeArrays& ra, const La
   if (want > ra.max_ranges) want = ra.max_ranges;
   const uint64_t tile = (uint64_t)kSortThreads * v.items;
   const uint64_t quantum = std::max<uint64_t>(tile, kRangeQuantum);
+  if (c.derive_ok && c.passes == 2) {  // key counts and key starts (derive mode)
+    err = cudaMemsetAsync(c.keyhist, 0, (size_t)65536 * 4, s);
+    if (err == cudaSuccess) err = cudaMemsetAsync(c.keystart, 0, ceil_div(c.n, 32) * 4, s);
+    if (err != cudaSuccess) return err;
+  }
   OneColumn g;
   g.c = c;
   g.range_rows = std::max<uint64_t>(ceil_div(ceil_div(c.n, want), quantum) * quantum, quantum);

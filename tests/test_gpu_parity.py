@@ -69,6 +69,16 @@ def test_random_columns(wah, kind, n):
     assert_same(wah.build_index(v), O.build(v), f"{kind}/{n}")
 
 
+@pytest.mark.parametrize("kind", ["uniform16", "few16", "zipf", "runs", "const", "two"])
+@pytest.mark.parametrize("n", [1, 30, 31, 33, 1000, 2048, 4096, 4097, 100_003, 1 << 20])
+def test_random_columns_bound16(wah, kind, n):
+    # a 16-bit bound: two digit passes; where both digits vary the build
+    # takes key starts from the full-key counts instead of reading keys
+    rng = np.random.default_rng(hash((kind, n, 16)) & 0xFFFFFFFF)
+    v = gen(kind, n, rng)
+    assert_same(wah.build_index(v, bound=65535), O.build(v), f"{kind}/{n}/b16")
+
+
 def test_config1_uniform_1m_with_bound(wah):
     # 1,048,576 uniform [0, 65535], seeded; bound given as the reference's -b
     rng = np.random.default_rng(1)
