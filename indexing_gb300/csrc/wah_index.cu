@@ -51,9 +51,11 @@ __device__ __forceinline__ uint32_t chunk_bit(uint32_t rid) {
   return (c << 5) | (rid - c * 31);
 }
 
-// Per-thread counters packed for one block scan: words | keys << 21.
-constexpr int kPackShift = 21;
-constexpr uint64_t kPackMask = (1ull << kPackShift) - 1;
+// A tile's words (<= 2 per row) and keys (<= 1 per row) pack into one
+// 32-bit scan value: words in the low 16 bits, keys in the high 16.
+constexpr int kPackShift = 16;
+constexpr uint32_t kPackMask = (1u << kPackShift) - 1;
+static_assert(2 * kBuildTile <= (int)kPackMask, "tile words fit 16 bits");
 
 // ---------------------------------------------------------------------------
 // Count: words, keys, segments per range.
@@ -234,7 +236,7 @@ struct EmitSmem {
   uint32_t words[kSkewed(2 * kBuildTile)];
   uint32_t keys[kSkewed(kBuildTile)];
   uint32_t offs[kSkewed(kBuildTile)];
-  uint64_t warp_tmp[kBuildThreads / 32 + 1];
+  uint32_t warp_tot[kBuildThreads / 32];  // the warps' packed (words, keys) totals
   uint64_t bar[2];
   int abort;
 };
@@ -419,14 +421,32 @@ __device__ __forceinline__ void build_emit(const G& g, const uint32_t* __restric
       if (headm & (1u << j)) acc = 0;
     }
 
-    uint64_t tile_agg;
-    const uint64_t my_prefix = block_exclusive_scan64<kBuildThreads>(
-        (uint64_t)nw | ((uint64_t)nk << kPackShift), &tile_agg, sm.warp_tmp);
-    const uint32_t tw = (uint32_t)(tile_agg & kPackMask);
-    const uint32_t tk = (uint32_t)((tile_agg >> kPackShift) & kPackMask);
+    // Tile scan of (words, keys): warp scans, the warps' totals through
+    // shared memory (read before the staging barrier below, written again
+    // only after the tile's closing barrier).
+    const uint32_t lane = tid & 31, warp = tid >> 5;
+    const uint32_t x = nw | (nk << kPackShift);
+    uint32_t incl = x;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, incl, d);
+      if (lane >= (uint32_t)d) incl += y;
+    }
+    if (lane == 31) sm.warp_tot[warp] = incl;
+    __syncthreads();
+    uint32_t before = 0, tile_agg = 0;
+#pragma unroll
+    for (int w = 0; w < kBuildThreads / 32; ++w) {
+      const uint32_t t = sm.warp_tot[w];
+      before += (uint32_t)w < warp ? t : 0u;
+      tile_agg += t;
+    }
+    const uint32_t my_prefix = before + incl - x;
+    const uint32_t tw = tile_agg & kPackMask;
+    const uint32_t tk = tile_agg >> kPackShift;
 
-    uint32_t pw = (uint32_t)(my_prefix & kPackMask);
-    uint32_t pk = (uint32_t)((my_prefix >> kPackShift) & kPackMask);
+    uint32_t pw = my_prefix & kPackMask;
+    uint32_t pk = my_prefix >> kPackShift;
 #pragma unroll
     for (int j = 0; j < kBuildItems; ++j) {
       if (headm & (1u << j)) {
