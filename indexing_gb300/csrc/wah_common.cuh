@@ -169,6 +169,34 @@ __device__ __forceinline__ void set_status(uint32_t* status, uint32_t code) {
   if (status) atomicCAS(status, 0u, code);
 }
 
+// Exclusive scan of one u32 per thread across a block of up to 256 threads
+// with one barrier: warp scans, then every thread adds up the totals of the
+// warps before its own.  The caller keeps a barrier between its reads of
+// s_warp here and the next call's writes.
+template <int THREADS>
+__device__ __forceinline__ uint32_t block_exclusive_scan_1b(uint32_t x, uint32_t* total,
+                                                            uint32_t* s_warp /* THREADS/32 */) {
+  static_assert(THREADS <= 256, "one pass over the warp totals");
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t incl = x;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, incl, d);
+    if (lane >= (uint32_t)d) incl += y;
+  }
+  if (lane == 31) s_warp[warp] = incl;
+  __syncthreads();
+  uint32_t before = 0, all = 0;
+#pragma unroll
+  for (int w = 0; w < THREADS / 32; ++w) {
+    const uint32_t t = s_warp[w];
+    before += (uint32_t)w < warp ? t : 0u;
+    all += t;
+  }
+  *total = all;
+  return before + incl - x;
+}
+
 // Exclusive scan of one u32 per thread across a block of THREADS threads.
 // Returns the thread's exclusive prefix; *total gets the block sum.
 template <int THREADS>

@@ -421,27 +421,11 @@ __device__ __forceinline__ void build_emit(const G& g, const uint32_t* __restric
       if (headm & (1u << j)) acc = 0;
     }
 
-    // Tile scan of (words, keys): warp scans, the warps' totals through
-    // shared memory (read before the staging barrier below, written again
-    // only after the tile's closing barrier).
-    const uint32_t lane = tid & 31, warp = tid >> 5;
-    const uint32_t x = nw | (nk << kPackShift);
-    uint32_t incl = x;
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-      const uint32_t y = __shfl_up_sync(0xffffffffu, incl, d);
-      if (lane >= (uint32_t)d) incl += y;
-    }
-    if (lane == 31) sm.warp_tot[warp] = incl;
-    __syncthreads();
-    uint32_t before = 0, tile_agg = 0;
-#pragma unroll
-    for (int w = 0; w < kBuildThreads / 32; ++w) {
-      const uint32_t t = sm.warp_tot[w];
-      before += (uint32_t)w < warp ? t : 0u;
-      tile_agg += t;
-    }
-    const uint32_t my_prefix = before + incl - x;
+    // Tile scan of (words, keys); the warp totals are read before the
+    // staging barrier below and written again after the tile's last one.
+    uint32_t tile_agg;
+    const uint32_t my_prefix = block_exclusive_scan_1b<kBuildThreads>(
+        nw | (nk << kPackShift), &tile_agg, sm.warp_tot);
     const uint32_t tw = tile_agg & kPackMask;
     const uint32_t tk = tile_agg >> kPackShift;
 

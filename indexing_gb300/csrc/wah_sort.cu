@@ -535,25 +535,25 @@ __global__ void __launch_bounds__(kSortThreads, 2)
     if (tid == 0 && i + 1 < ntiles && hi - (base + TILE) >= TILE)
       fetch_tile(sm.in_keys[cur ^ 1], sm.in_rids[cur ^ 1], &sm.bar[cur ^ 1], kin, rin,
                  base + TILE, TILE, k16_in);
-    // Zero the warp counters (the previous tile's last reads were fenced).
+    // Each warp zeroes its own counters (every read of them in the previous
+    // tile came before the barrier that closed it).
     {
-      uint4* w4 = reinterpret_cast<uint4*>(&sm.whist[0][0][0]);
-      for (uint32_t k = tid; k < 2 * kSortWarps * kRadix / 4; k += kSortThreads)
-        w4[k] = make_uint4(0, 0, 0, 0);
+      uint4* w4 = reinterpret_cast<uint4*>(whA);
+#pragma unroll
+      for (uint32_t k = lane; k < 2 * kRadix / 4; k += 32) w4[k] = make_uint4(0, 0, 0, 0);
+      __syncwarp();
     }
     uint32_t key[ITEMS];
     if (valid == TILE) {
       // phases of each buffer's barrier complete in turn; the parity of the
       // next one is tracked per buffer (a tile read with plain loads uses
-      // none).  One thread waits for the copy; the block barrier then hands
-      // its completion (and the zeroed counters) to every thread.
-      if (tid == 0 && !mbar_wait_bounded(&sm.bar[cur], (phase_bits >> cur) & 1u)) {
+      // none).  Every thread waits for the copy itself.
+      if (!mbar_wait_bounded(&sm.bar[cur], (phase_bits >> cur) & 1u)) {
         set_status(status, WAH_ETIMEOUT);
         sm.abort = 1;
       }
       phase_bits ^= 1u << cur;
     }
-    __syncthreads();
     if (valid == TILE) {
       if (k16_in) {
         const uint16_t* kp = reinterpret_cast<const uint16_t*>(sm.in_keys[cur]) + row0;
@@ -613,7 +613,8 @@ __global__ void __launch_bounds__(kSortThreads, 2)
       count += cnt[w];
     }
     uint32_t tile_total;
-    const uint32_t lstart = block_exclusive_scan<kSortThreads>(count, &tile_total, sm.warp_tmp);
+    // (warp totals read here, written again after this tile's later barriers)
+    const uint32_t lstart = block_exclusive_scan_1b<kSortThreads>(count, &tile_total, sm.warp_tmp);
     {
       uint32_t run = lstart;
 #pragma unroll
