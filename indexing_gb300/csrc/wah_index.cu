@@ -60,24 +60,23 @@ static_assert(2 * kBuildTile <= (int)kPackMask, "tile words fit 16 bits");
 // ---------------------------------------------------------------------------
 // Count: words, keys, segments per range.
 // ---------------------------------------------------------------------------
-// vh: the row starts a key (derive mode reads it from the key-start bits)
-__device__ __forceinline__ void count_row_h(bool vh, uint32_t c, uint32_t pc, uint32_t& words,
-                                            uint32_t& keys, uint32_t& segs) {
-  const bool h = vh || c != pc;
-  const uint32_t fill = vh ? c : c - pc - 1;
-  words += h ? 1u + (fill != 0) : 0u;
-  keys += vh;
-  segs += h;
+// Words and segments of one sorted row.  vh: the row starts a key; c, pc:
+// the chunk ids of the row and of the row before (pc <= c within a key).
+// x = 0: the row's chunk continues the segment (no word); x = 1: a new chunk
+// right after the last one (literal only); x >= 2: a zero fill, then the
+// literal.  A key's first row has a fill unless its chunk is 0 (x = c + 1).
+__device__ __forceinline__ void count_words(bool vh, uint32_t c, uint32_t pc, uint32_t& words,
+                                            uint32_t& segs) {
+  const uint32_t x = vh ? c + 1 : c - pc;
+  words += min(x, 2u);
+  segs += min(x, 1u);
 }
 
 __device__ __forceinline__ void count_row(uint32_t v, uint32_t c, uint32_t pv, uint32_t pc,
                                           uint32_t& words, uint32_t& keys, uint32_t& segs) {
   const bool vh = v != pv;
-  const bool h = vh || c != pc;
-  const uint32_t fill = vh ? c : c - pc - 1;
-  words += h ? 1u + (fill != 0) : 0u;
+  count_words(vh, c, pc, words, segs);
   keys += vh;
-  segs += h;
 }
 
 template <class G>
@@ -106,10 +105,11 @@ __global__ void __launch_bounds__(kHistThreads)
       const uint32_t up = __shfl_up_sync(0xffffffffu, r4.w, 1);
       const uint32_t pc = (lane == 0 ? pr : up) / 31;
       const uint32_t c0 = r4.x / 31, c1 = r4.y / 31, c2 = r4.z / 31, c3 = r4.w / 31;
-      count_row_h(bits & 1u, c0, pc, words, keys, segs);
-      count_row_h((bits >> 1) & 1u, c1, c0, words, keys, segs);
-      count_row_h((bits >> 2) & 1u, c2, c1, words, keys, segs);
-      count_row_h((bits >> 3) & 1u, c3, c2, words, keys, segs);
+      count_words(bits & 1u, c0, pc, words, segs);
+      count_words((bits >> 1) & 1u, c1, c0, words, segs);
+      count_words((bits >> 2) & 1u, c2, c1, words, segs);
+      count_words((bits >> 3) & 1u, c3, c2, words, segs);
+      keys += __popc(bits & 0xFu);
     };
     uint64_t k = warp;
     for (; k + (kHistUnroll - 1) * kHistWarps < chunks; k += kHistUnroll * kHistWarps) {
@@ -134,7 +134,9 @@ __global__ void __launch_bounds__(kHistThreads)
       for (uint64_t p = lo + chunks * 128 + lane; p < hi; p += 32) {
         const uint32_t cc = sr[p] / 31;
         const uint32_t pc = p > 0 ? sr[p - 1] / 31 : 0u;
-        count_row_h((ks[p >> 5] >> (p & 31)) & 1u, cc, pc, words, keys, segs);
+        const uint32_t vh = (ks[p >> 5] >> (p & 31)) & 1u;
+        count_words(vh, cc, pc, words, segs);
+        keys += vh;
       }
     }
   } else {
@@ -385,12 +387,13 @@ __device__ __forceinline__ void build_emit(const G& g, const uint32_t* __restric
       const uint32_t c = cb[j] >> 5;
       const bool ok = full || first + j < valid;
       const bool vh = derive ? ((kbits >> j) & 1u) != 0 : v[j] != pv;
-      const bool h = ok && (vh || c != pc);
-      fills[j] = vh ? c : c - pc - 1;
-      if (h) {
+      // x as in count_words: 0 continues the segment, else the fill is x - 1
+      const uint32_t x = vh ? c + 1 : c - pc;
+      fills[j] = x - 1;
+      if (ok && x != 0) {
         headm |= 1u << j;
         if (vh) vheadm |= 1u << j;
-        nw += 1 + (fills[j] != 0);
+        nw += min(x, 2u);
       }
       pv = v[j];
       pc = c;
