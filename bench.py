@@ -67,6 +67,9 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n", type=int, default=268_435_456)
     ap.add_argument("--card", type=int, default=65536, help="values uniform in [0, card)")
+    ap.add_argument("--bound", type=int, default=None,
+                    help="bound given to the build (default card - 1; 0: the build scans "
+                         "the column for its largest value)")
     ap.add_argument("--seed", type=int, default=20170101)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-skewed", action="store_true")
@@ -652,7 +655,7 @@ def main():
         if lib.wah_set_tuning(args.sort_items) != 0:
             raise SystemExit(f"unsupported --sort-items {args.sort_items}")
     n, card = args.n, args.card
-    bound = card - 1
+    bound = card - 1 if args.bound is None else args.bound
     tuned = None
     if not args.no_autotune and not args.sort_items:
         t, cached = wah.autotune(n, bound, args.tune_cache)

@@ -52,7 +52,7 @@ struct WahCtrl {
   int32_t derive;                     // key starts replace the sorted keys (ColumnView)
   uint32_t key_or;                    // OR of all keys (range check vs bound)
   uint32_t key_nor;                   // OR of the complements: bits some key has clear
-  uint32_t pad[1];
+  int32_t narrow;                     // every key below 2^16: 16-bit keys between passes
 };
 
 
@@ -326,12 +326,12 @@ __host__ __device__ __forceinline__ const uint32_t* sel_keys(const ColumnView& c
   return s == kSelInput ? c.input : (s == kSelA ? c.keys_a : c.keys_b);
 }
 // A sort buffer between two digit passes holds 16-bit keys when every key
-// fits 16 bits (at most two digit passes, the bound checked by the sort
-// plan); the caller's input and the last pass's output (read by the index
-// build) keep 32-bit keys.  A narrow buffer uses the first half of its u32
-// array.  Valid once the sort plan has run.
+// fits 16 bits (the OR of the keys, whatever the bound); the caller's input
+// and the last pass's output (read by the index build) keep 32-bit keys.  A
+// narrow buffer uses the first half of its u32 array.  Valid once the sort
+// plan has run.
 __device__ __forceinline__ bool narrow_keys(const ColumnView& c, int s) {
-  return c.passes <= 2 && s != kSelInput && s != c.ctrl->final_sel;
+  return c.ctrl->narrow && s != kSelInput && s != c.ctrl->final_sel;
 }
 __host__ __device__ __forceinline__ const uint32_t* sel_rids(const ColumnView& c, int s) {
   return s == kSelInput ? c.input_rids : (s == kSelA ? c.rids_a : c.rids_b);

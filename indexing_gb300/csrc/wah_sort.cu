@@ -288,7 +288,10 @@ __global__ void __launch_bounds__(kRadix) k_sort_plan(G g) {
     const uint32_t varying = ctrl->key_or & ctrl->key_nor;
     int s_active[kDigits];
     for (int p = 0; p < kDigits; ++p) s_active[p] = digit8(varying, p) != 0;
-    ctrl->derive = c.derive_ok && passes == 2 && s_active[0] && s_active[1];
+    // every key below 2^16 (digits 2 and 3 then inactive): 16-bit keys
+    // between the passes, and key starts when both low digits vary
+    ctrl->narrow = (ctrl->key_or >> 16) == 0;
+    ctrl->derive = c.derive_ok && ctrl->narrow && s_active[0] && s_active[1];
     // A set bit above the digits the bound allows: the sort would be wrong.
     if (passes < kDigits && (ctrl->key_or >> (passes * kRadixBits)) != 0)
       set_status(status, WAH_ERANGE);
@@ -735,7 +738,7 @@ cudaError_t launch_sort_t(const G& g, uint32_t ncols, uint32_t ranges, const Ran
       ++*launches;
     }
     if constexpr (std::is_same<G, OneColumn>::value) {
-      if (p == 1 && g.c.derive_ok && g.c.passes == 2) {  // works only in derive mode
+      if (p == 1 && g.c.derive_ok) {  // works only in derive mode
         k_key_starts<G><<<kKeyStartCtas, kKeyStartThreads, 0, s>>>(g);
         ++*launches;
       }
@@ -765,7 +768,7 @@ cudaError_t launch_sort_one(const ColumnView& c, const RangeArrays& ra, const La
   if (want > ra.max_ranges) want = ra.max_ranges;
   const uint64_t tile = (uint64_t)kSortThreads * v.items;
   const uint64_t quantum = std::max<uint64_t>(tile, kRangeQuantum);
-  if (c.derive_ok && c.passes == 2) {  // key counts and key starts (derive mode)
+  if (c.derive_ok && c.passes >= 2) {  // key counts and key starts (derive mode)
     err = cudaMemsetAsync(c.keyhist, 0, (size_t)65536 * 4, s);
     if (err == cudaSuccess) err = cudaMemsetAsync(c.keystart, 0, ceil_div(c.n, 32) * 4, s);
     if (err != cudaSuccess) return err;
