@@ -32,8 +32,8 @@ constexpr int kCountCtasPerRange = 2;
 
 
 // Fused index build: 256 threads x 8 rows, blocked.
-constexpr int kBuildThreads = 256;
-constexpr int kBuildItems = 8;
+constexpr int kBuildThreads = 128;
+constexpr int kBuildItems = 16;
 constexpr int kBuildTile = kBuildThreads * kBuildItems;  // 2048 rows
 
 constexpr int kHistThreads = 256;

@@ -41,10 +41,10 @@ constexpr int kLookAhead = 30;  // rows after a tile that can continue its last 
 constexpr int kWinBehind = 4;   // window starts 4 rows before the tile (16-byte aligned)
 constexpr int kWinRows = kWinBehind + kBuildTile + 32;  // rows fetched per tile
 
-// Staging index skew: position i lives at i + i/16, so threads writing runs
-// that start ~16 words apart hit different banks.
-__device__ __forceinline__ uint32_t skew(uint32_t i) { return i + (i >> 4); }
-constexpr int kSkewed(int n) { return n + n / 16 + 1; }
+// Staging index skew: position i lives at i + i/32, so threads writing runs
+// that start ~2 x kBuildItems = 32 words apart hit different banks.
+__device__ __forceinline__ uint32_t skew(uint32_t i) { return i + (i >> 5); }
+constexpr int kSkewed(int n) { return n + n / 32 + 1; }
 
 __device__ __forceinline__ uint32_t chunk_bit(uint32_t rid) {
   const uint32_t c = rid / 31;
@@ -345,23 +345,26 @@ __device__ __forceinline__ void build_emit(const G& g, const uint32_t* __restric
       __syncthreads();
     }
 
-    // This thread's 8 rows from the window (two 16-byte loads per array).
+    // This thread's rows from the window (16-byte loads).
+    static_assert(kBuildItems % 4 == 0, "whole 16-byte loads");
     uint32_t v[kBuildItems], cb[kBuildItems];
     {
       const uint4* r4 = reinterpret_cast<const uint4*>(wr + kWinBehind + first);
-      const uint4 b0 = r4[0], b1 = r4[1];
-      if (!derive) {
-        const uint4* v4 = reinterpret_cast<const uint4*>(wv + kWinBehind + first);
-        const uint4 a0 = v4[0], a1 = v4[1];
-        v[0] = a0.x; v[1] = a0.y; v[2] = a0.z; v[3] = a0.w;
-        v[4] = a1.x; v[5] = a1.y; v[6] = a1.z; v[7] = a1.w;
-      } else {
+      const uint4* v4 = reinterpret_cast<const uint4*>(wv + kWinBehind + first);
 #pragma unroll
-        for (int j = 0; j < kBuildItems; ++j) v[j] = 0;
+      for (int q = 0; q < kBuildItems / 4; ++q) {
+        const uint4 b = r4[q];
+        cb[4 * q + 0] = chunk_bit(b.x);
+        cb[4 * q + 1] = chunk_bit(b.y);
+        cb[4 * q + 2] = chunk_bit(b.z);
+        cb[4 * q + 3] = chunk_bit(b.w);
+        if (!derive) {
+          const uint4 a = v4[q];
+          v[4 * q + 0] = a.x; v[4 * q + 1] = a.y; v[4 * q + 2] = a.z; v[4 * q + 3] = a.w;
+        } else {
+          v[4 * q + 0] = v[4 * q + 1] = v[4 * q + 2] = v[4 * q + 3] = 0;
+        }
       }
-      cb[0] = chunk_bit(b0.x); cb[1] = chunk_bit(b0.y); cb[2] = chunk_bit(b0.z);
-      cb[3] = chunk_bit(b0.w); cb[4] = chunk_bit(b1.x); cb[5] = chunk_bit(b1.y);
-      cb[6] = chunk_bit(b1.z); cb[7] = chunk_bit(b1.w);
     }
     const bool full = valid == kBuildTile;
     // rows that exist from the tile start: rows past the range end but before
@@ -376,9 +379,11 @@ __device__ __forceinline__ void build_emit(const G& g, const uint32_t* __restric
       pv = ~v[0];
       pc = 0;
     }
-    // derive mode: which of this thread's 8 rows start a key (one bit word;
-    // the row offset is a multiple of 8)
-    const uint32_t kbits = derive ? (wv[first >> 5] >> (first & 31)) & 0xFFu : 0u;
+    // derive mode: which of this thread's rows start a key (one bit word;
+    // the row offset is a multiple of the rows per thread, which divides 32)
+    static_assert(32 % kBuildItems == 0, "a thread's key-start bits in one word");
+    constexpr uint32_t kItemMask = (1u << kBuildItems) - 1;
+    const uint32_t kbits = derive ? (wv[first >> 5] >> (first & 31)) & kItemMask : 0u;
 
     uint32_t headm = 0, vheadm = 0, fills[kBuildItems];
     uint32_t nw = 0;

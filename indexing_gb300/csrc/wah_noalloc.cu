@@ -8,7 +8,7 @@
 // add a device-wide synchronisation to every request.  They still provide the
 // column and the output buffers; this entry point takes the rest of what the
 // build needs (the sort ping-pong buffers, digit histograms, range counters
-// and look-back words) from one fixed array in this library's device image.
+// and key-start bits) from one fixed array in this library's device image.
 //
 // The array is a file-scope __device__ variable of kNoAllocBytes, so every
 // GPU that loads the library holds it until the process exits.  Columns of up
@@ -27,7 +27,7 @@
 
 namespace {
 
-// Workspace of wah_build for WAH_NOALLOC_MAX_ROWS rows (21.0 MiB), rounded up.
+// Workspace of wah_build for WAH_NOALLOC_MAX_ROWS rows (21.4 MiB), rounded up.
 constexpr size_t kNoAllocBytes = (size_t)22 << 20;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
