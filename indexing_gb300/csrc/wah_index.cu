@@ -45,6 +45,7 @@ constexpr int kWinRows = kWinBehind + kBuildTile + 32;  // rows fetched per tile
 // that start ~2 x kBuildItems = 32 words apart hit different banks.
 __device__ __forceinline__ uint32_t skew(uint32_t i) { return i + (i >> 5); }
 constexpr int kSkewed(int n) { return n + n / 32 + 1; }
+constexpr int kStagedWords = kSkewed(2 * kBuildTile);  // a tile's words, skewed
 
 __device__ __forceinline__ uint32_t chunk_bit(uint32_t rid) {
   const uint32_t c = rid / 31;
@@ -233,15 +234,22 @@ __global__ void __launch_bounds__(kBuildScanThreads)
 // Emit.
 // ---------------------------------------------------------------------------
 struct EmitSmem {
-  uint32_t win_v[2][kWinRows];  // window rows base-4 .. base+TILE+31
-  uint32_t win_r[2][kWinRows];
-  uint32_t words[kSkewed(2 * kBuildTile)];
+  // Per buffer: the window's keys (or key-start bits) and row ids, rows
+  // base-4 .. base+TILE+31.  Once every thread has its rows (the tile scan's
+  // barrier), the current buffer stages the tile's words in skewed order.
+  struct Win {
+    uint32_t v[kWinRows];
+    uint32_t r[kWinRows];
+    uint32_t pad[(kStagedWords - 2 * kWinRows + 3) / 4 * 4];
+  } win[2];
   uint32_t keys[kSkewed(kBuildTile)];
   uint32_t offs[kSkewed(kBuildTile)];
   uint32_t warp_tot[kBuildThreads / 32];  // the warps' packed (words, keys) totals
   uint64_t bar[2];
   int abort;
 };
+static_assert(sizeof(EmitSmem::Win) >= kStagedWords * sizeof(uint32_t), "staging fits a buffer");
+static_assert(sizeof(EmitSmem::Win) % 16 == 0, "16-byte aligned bulk-copy targets");
 
 // A tile's window can come by bulk copy when all its rows exist and it does
 // not start before row 0.
@@ -298,7 +306,7 @@ __device__ __forceinline__ void build_emit(const G& g, const uint32_t* __restric
     sm.abort = 0;
     fence_mbar_init();
     if (window_bulk(lo, n))
-      fetch_window(sm.win_v[0], sm.win_r[0], &sm.bar[0], sv, sr, ks, lo, derive);
+      fetch_window(sm.win[0].v, sm.win[0].r, &sm.bar[0], sv, sr, ks, lo, derive);
   }
   __syncthreads();
 
@@ -309,10 +317,12 @@ __device__ __forceinline__ void build_emit(const G& g, const uint32_t* __restric
     const uint64_t base = lo + (uint64_t)i * kBuildTile;
     const uint32_t valid = hi - base < kBuildTile ? (uint32_t)(hi - base) : kBuildTile;
     if (tid == 0 && i + 1 < ntiles && window_bulk(base + kBuildTile, n))
-      fetch_window(sm.win_v[cur ^ 1], sm.win_r[cur ^ 1], &sm.bar[cur ^ 1], sv, sr, ks,
+      fetch_window(sm.win[cur ^ 1].v, sm.win[cur ^ 1].r, &sm.bar[cur ^ 1], sv, sr, ks,
                    base + kBuildTile, derive);
-    uint32_t* wv = sm.win_v[cur];
-    uint32_t* wr = sm.win_r[cur];
+    uint32_t* wv = sm.win[cur].v;
+    uint32_t* wr = sm.win[cur].r;
+    // the tile's staged words, in the same buffer once its rows are read
+    uint32_t* words = sm.win[cur].v;
     // rows of the window that exist, counted from the tile start
     const uint64_t left = n - base;
     const uint32_t wend = left < (uint64_t)(kBuildTile + kLookAhead)
@@ -447,8 +457,8 @@ __device__ __forceinline__ void build_emit(const G& g, const uint32_t* __restric
           sm.offs[skew(pk)] = run_w + pw;
           ++pk;
         }
-        if (fills[j]) sm.words[skew(pw++)] = fills[j];
-        sm.words[skew(pw++)] = lits[j];
+        if (fills[j]) words[skew(pw++)] = fills[j];
+        words[skew(pw++)] = lits[j];
       }
     }
     __syncthreads();
@@ -460,24 +470,24 @@ __device__ __forceinline__ void build_emit(const G& g, const uint32_t* __restric
         // words up to the next 16-byte boundary of the index, then groups of
         // four with one 16-byte store each, then the rest
         const uint32_t head = ((4u - (run_w & 3u)) & 3u) < tw ? ((4u - (run_w & 3u)) & 3u) : tw;
-        if (tid < head) out_index[run_w + tid] = sm.words[skew(tid)];
+        if (tid < head) out_index[run_w + tid] = words[skew(tid)];
         const uint32_t groups = (tw - head) >> 2;
         for (uint32_t g = tid; g < groups; g += kBuildThreads) {
           const uint32_t k = head + 4 * g;
           uint4 q;
-          q.x = sm.words[skew(k)];
-          q.y = sm.words[skew(k + 1)];
-          q.z = sm.words[skew(k + 2)];
-          q.w = sm.words[skew(k + 3)];
+          q.x = words[skew(k)];
+          q.y = words[skew(k + 1)];
+          q.z = words[skew(k + 2)];
+          q.w = words[skew(k + 3)];
           *reinterpret_cast<uint4*>(out_index + run_w + k) = q;
         }
         const uint32_t tail = head + 4 * groups;
-        if (tid < tw - tail) out_index[run_w + tail + tid] = sm.words[skew(tail + tid)];
+        if (tid < tw - tail) out_index[run_w + tail + tid] = words[skew(tail + tid)];
       } else {
         for (uint32_t k = tid; k < tw; k += kBuildThreads) {
           const uint64_t pos = (uint64_t)run_w + k;
           if (pos < index_cap)
-            out_index[pos] = sm.words[skew(k)];
+            out_index[pos] = words[skew(k)];
           else
             overflow = true;
         }
@@ -500,7 +510,7 @@ __device__ __forceinline__ void build_emit(const G& g, const uint32_t* __restric
 }
 
 template <class G>
-__global__ void __launch_bounds__(kBuildThreads, 3)
+__global__ void __launch_bounds__(kBuildThreads, 4)
     k_build_emit(G g, const uint32_t* __restrict__ range_first) {
   extern __shared__ __align__(128) unsigned char smem_raw[];
   EmitSmem& sm = *reinterpret_cast<EmitSmem*>(smem_raw);
