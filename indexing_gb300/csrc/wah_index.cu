@@ -90,49 +90,55 @@ __global__ void __launch_bounds__(kHistThreads)
   const uint32_t* __restrict__ sv = sel_keys(col, s);
   const uint32_t* __restrict__ sr = sel_rids(col, s);
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  // part q of the range (parts start on multiples of 4 rows: aligned loads)
-  const uint64_t part = ((rv.hi - rv.lo) / kCountCtasPerRange) & ~(uint64_t)3;
+  // part q of the range (parts start on multiples of 8 rows: aligned loads,
+  // and a lane's 8 rows in one key-start bit word)
+  const uint64_t part = ((rv.hi - rv.lo) / kCountCtasPerRange) & ~(uint64_t)7;
   const uint64_t lo = rv.lo + q * part;
   const uint64_t hi = q + 1 == kCountCtasPerRange ? rv.hi : lo + part;
 
   uint32_t words = 0, keys = 0, segs = 0;
   const uint64_t chunks = (hi - lo) / 128;  // 32 lanes x 4 rows
   if (col.fixed_sel < 0 && col.ctrl->derive) {
-    // key heads from the key-start bits (rows p..p+3 share one bit word),
-    // chunks from the row ids; no keys read
+    // key heads from the key-start bits (a lane's 8 rows share one bit
+    // word), chunks from the row ids; no keys read.  Loads of kHistUnroll
+    // chunks of 256 rows are issued together, then counted.
     const uint32_t* __restrict__ ks = col.keystart;
-    // loads of kHistUnroll chunks issued together, then counted
-    auto count4 = [&](const uint4& r4, uint32_t bits, uint32_t pr) {
-      const uint32_t up = __shfl_up_sync(0xffffffffu, r4.w, 1);
-      const uint32_t pc = (lane == 0 ? pr : up) / 31;
-      const uint32_t c0 = r4.x / 31, c1 = r4.y / 31, c2 = r4.z / 31, c3 = r4.w / 31;
-      count_words(bits & 1u, c0, pc, words, segs);
-      count_words((bits >> 1) & 1u, c1, c0, words, segs);
-      count_words((bits >> 2) & 1u, c2, c1, words, segs);
-      count_words((bits >> 3) & 1u, c3, c2, words, segs);
-      keys += __popc(bits & 0xFu);
+    auto count8 = [&](const uint4& a, const uint4& b, uint32_t bits, uint32_t pr) {
+      const uint32_t up = __shfl_up_sync(0xffffffffu, b.w, 1);
+      uint32_t pc = (lane == 0 ? pr : up) / 31;
+      const uint32_t r[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const uint32_t cj = r[j] / 31;
+        count_words((bits >> j) & 1u, cj, pc, words, segs);
+        pc = cj;
+      }
+      keys += __popc(bits & 0xFFu);
     };
+    const uint64_t chunks8 = (hi - lo) / 256;  // 32 lanes x 8 rows
     uint64_t k = warp;
-    for (; k + (kHistUnroll - 1) * kHistWarps < chunks; k += kHistUnroll * kHistWarps) {
-      uint4 r4[kHistUnroll];
+    for (; k + (kHistUnroll - 1) * kHistWarps < chunks8; k += kHistUnroll * kHistWarps) {
+      uint4 ra[kHistUnroll], rb[kHistUnroll];
       uint32_t bits[kHistUnroll], pr[kHistUnroll];
 #pragma unroll
       for (int u = 0; u < kHistUnroll; ++u) {
-        const uint64_t p = lo + (k + u * kHistWarps) * 128 + lane * 4;
-        r4[u] = ld_stream_v4(reinterpret_cast<const uint4*>(sr + p));
+        const uint64_t p = lo + (k + u * kHistWarps) * 256 + lane * 8;
+        ra[u] = ld_stream_v4(reinterpret_cast<const uint4*>(sr + p));
+        rb[u] = ld_stream_v4(reinterpret_cast<const uint4*>(sr + p + 4));
         bits[u] = ks[p >> 5] >> (p & 31);
         pr[u] = (lane == 0 && p > 0) ? sr[p - 1] : 0u;
       }
 #pragma unroll
-      for (int u = 0; u < kHistUnroll; ++u) count4(r4[u], bits[u], pr[u]);
+      for (int u = 0; u < kHistUnroll; ++u) count8(ra[u], rb[u], bits[u], pr[u]);
     }
-    for (; k < chunks; k += kHistWarps) {
-      const uint64_t p = lo + k * 128 + lane * 4;
-      const uint4 r4 = ld_stream_v4(reinterpret_cast<const uint4*>(sr + p));
-      count4(r4, ks[p >> 5] >> (p & 31), (lane == 0 && p > 0) ? sr[p - 1] : 0u);
+    for (; k < chunks8; k += kHistWarps) {
+      const uint64_t p = lo + k * 256 + lane * 8;
+      count8(ld_stream_v4(reinterpret_cast<const uint4*>(sr + p)),
+             ld_stream_v4(reinterpret_cast<const uint4*>(sr + p + 4)), ks[p >> 5] >> (p & 31),
+             (lane == 0 && p > 0) ? sr[p - 1] : 0u);
     }
     if (warp == 0) {
-      for (uint64_t p = lo + chunks * 128 + lane; p < hi; p += 32) {
+      for (uint64_t p = lo + chunks8 * 256 + lane; p < hi; p += 32) {
         const uint32_t cc = sr[p] / 31;
         const uint32_t pc = p > 0 ? sr[p - 1] / 31 : 0u;
         const uint32_t vh = (ks[p >> 5] >> (p & 31)) & 1u;
