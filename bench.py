@@ -89,7 +89,8 @@ def parse():
                     help="builds in flight in the end-to-end leg")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--sort-items", type=int, default=0,
-                    help="radix scatter tuning: rows per thread | peer-mask flags (0: library default)")
+                    help="radix scatter tuning: rows per thread | peer-mask flags, optionally "
+                         "| (later passes' shape << 16) (0: library default)")
     ap.add_argument("--cpu-sample", type=int, default=1 << 23,
                     help="rows per oracle build in the CPU legs")
     return ap.parse_args()

@@ -394,11 +394,14 @@ uint32_t wah_last_launch_count(void);
 /* Tile shape of the radix digit passes: rows per thread (8, 12 or 16;
  * 256 threads per tile), optionally OR WAH_TUNE_MATCH to build the digit
  * peer masks with match.any instead of ballots, or WAH_TUNE_HYBRID to build
- * 3/8 of them with match.any and the rest with ballots.  Process-wide; set by the
- * autotuner or the caller before builds are enqueued.  The reference
+ * 3/8 of them with match.any and the rest with ballots.  That shape applies
+ * to digit pass 0; WAH_TUNE_LATER(shape) ORed in gives one-column builds a
+ * different shape for the later passes (0: the same).  Process-wide; set by
+ * the autotuner or the caller before builds are enqueued.  The reference
  * hard-codes its radix shape (src/phases.cpp:445-453). */
 #define WAH_TUNE_MATCH 0x100
 #define WAH_TUNE_HYBRID 0x200
+#define WAH_TUNE_LATER(shape) ((shape) << 16)
 int wah_set_tuning(int sort_items);
 int wah_get_tuning(void);
 

@@ -52,8 +52,12 @@ int cuda_status(cudaError_t e) {
 LaunchOpts launch_opts(int max_passes, cudaEvent_t* events) {
   LaunchOpts o;
   const int t = g_tuning.load(std::memory_order_relaxed);
-  o.sort_items = t & 0xff;
-  o.sort_peers = (t & WAH_TUNE_MATCH) ? 1 : (t & WAH_TUNE_HYBRID) ? 2 : 0;
+  const int first = t & 0xffff;
+  const int later = (t >> 16) & 0xffff ? (t >> 16) & 0xffff : first;
+  o.sort_items = first & 0xff;
+  o.sort_peers = (first & WAH_TUNE_MATCH) ? 1 : (first & WAH_TUNE_HYBRID) ? 2 : 0;
+  o.later_items = later & 0xff;
+  o.later_peers = (later & WAH_TUNE_MATCH) ? 1 : (later & WAH_TUNE_HYBRID) ? 2 : 0;
   o.max_passes = max_passes;
   o.sm_count = sm_count_current();
   o.events = events;
@@ -156,11 +160,19 @@ size_t wah_workspace_bytes(uint64_t n, uint32_t /*bound*/) { return ws_layout(n)
 
 uint32_t wah_last_launch_count(void) { return g_last_launches; }
 
+// One tile shape: rows per thread | peer mode flag.
+static bool valid_shape(int t) {
+  const int items = t & 0xff;
+  if (items != 8 && items != 12 && items != 16) return false;
+  if ((t & WAH_TUNE_MATCH) && (t & WAH_TUNE_HYBRID)) return false;
+  return (t & ~(0xff | WAH_TUNE_MATCH | WAH_TUNE_HYBRID)) == 0;
+}
+
 int wah_set_tuning(int sort_items) {
-  const int items = sort_items & 0xff;
-  if (items != 8 && items != 12 && items != 16) return WAH_EINVAL;
-  if ((sort_items & WAH_TUNE_MATCH) && (sort_items & WAH_TUNE_HYBRID)) return WAH_EINVAL;
-  if (sort_items & ~(0xff | WAH_TUNE_MATCH | WAH_TUNE_HYBRID)) return WAH_EINVAL;
+  if (sort_items < 0) return WAH_EINVAL;
+  const int later = (sort_items >> 16) & 0xffff;
+  if (!valid_shape(sort_items & 0xffff) || (later != 0 && !valid_shape(later)))
+    return WAH_EINVAL;
   g_tuning.store(sort_items, std::memory_order_relaxed);
   return WAH_OK;
 }

@@ -26,6 +26,7 @@
 //                      out run by run at the range's running bin offsets.  The
 //                      first active pass takes rid = row index.
 #include <algorithm>
+#include <numeric>
 #include <type_traits>
 
 #include "wah_common.cuh"
@@ -431,7 +432,8 @@ struct ScatterSmem {
   uint32_t in_keys[2][kSortThreads * ITEMS];
   uint32_t in_rids[2][kSortThreads * ITEMS];
   uint32_t out_rids[kSortThreads * ITEMS];
-  uint32_t whist[kSortWarps][2][kRadix];  // per-warp, per-half counters
+  // per-warp, per-half counters (16-bit: at most a tile's rows, < 2^16)
+  uint16_t whist[kSortWarps][2][kRadix];
   uint32_t run_off[kRadix];               // range's next free position per bin
   uint32_t bin_base[kRadix];              // run_off - tile-local bin start
   uint32_t warp_tmp[kSortWarps + 1];
@@ -482,7 +484,7 @@ __host__ __device__ constexpr int kHybridMatchItems(int items) {
   return items * WAH_HYBRID_MATCH_NUM / 8;
 }
 template <int ITEMS, int PEERS, class G>
-__global__ void __launch_bounds__(kSortThreads, 2)
+__global__ void __launch_bounds__(kSortThreads, ITEMS <= 12 ? 3 : 2)
     k_radix_scatter(G g, int pass, const uint32_t* __restrict__ range_start) {
   constexpr uint32_t TILE = kSortThreads * ITEMS;
   constexpr int HALF = ITEMS / 2;
@@ -524,8 +526,9 @@ __global__ void __launch_bounds__(kSortThreads, 2)
 
   const uint32_t row0 = warp * 32 * ITEMS + lane;  // tile row of item 0
   const uint32_t lt = lanemask_lt(), gt = lanemask_gt();
-  uint32_t* whA = sm.whist[warp][0];
-  uint32_t* whB = sm.whist[warp][1];
+  uint16_t* whA = sm.whist[warp][0];
+  uint16_t* whB = sm.whist[warp][1];
+  static_assert(kSortThreads * ITEMS < 65536, "tile rows fit the 16-bit counters");
   uint32_t phase_bits = 0;  // parity of the next phase of bar[0], bar[1]
 
   for (uint32_t i = 0; i < ntiles; ++i) {
@@ -543,7 +546,7 @@ __global__ void __launch_bounds__(kSortThreads, 2)
     {
       uint4* w4 = reinterpret_cast<uint4*>(whA);
 #pragma unroll
-      for (uint32_t k = lane; k < 2 * kRadix / 4; k += 32) w4[k] = make_uint4(0, 0, 0, 0);
+      for (uint32_t k = lane; k < 2 * kRadix * 2 / 16; k += 32) w4[k] = make_uint4(0, 0, 0, 0);
       __syncwarp();
     }
     uint32_t key[ITEMS];
@@ -596,8 +599,8 @@ __global__ void __launch_bounds__(kSortThreads, 2)
       const uint32_t ca = whA[da];
       const uint32_t cb = whB[db];
       __syncwarp();
-      if ((pa & gt) == 0) whA[da] = ca + __popc(pa);
-      if ((pb & gt) == 0) whB[db] = cb + __popc(pb);
+      if ((pa & gt) == 0) whA[da] = (uint16_t)(ca + __popc(pa));
+      if ((pb & gt) == 0) whB[db] = (uint16_t)(cb + __popc(pb));
       __syncwarp();
       rank[j] = ca + __popc(pa & lt);
       rank[j + HALF] = cb + __popc(pb & lt);
@@ -622,7 +625,7 @@ __global__ void __launch_bounds__(kSortThreads, 2)
       uint32_t run = lstart;
 #pragma unroll
       for (int w = 0; w < kSortWarps; ++w) {
-        sm.whist[w][0][b] = run;
+        sm.whist[w][0][b] = (uint16_t)run;
         run += cnt[w];
       }
     }
@@ -695,8 +698,8 @@ SortVariant<G> sort_variant(int items, int peers) {
 }
 
 template <class G>
-cudaError_t scatter_variant(const LaunchOpts& o, SortVariant<G>* v, int* per_sm) {
-  *v = sort_variant<G>(o.sort_items, o.sort_peers);
+cudaError_t scatter_variant(int items, int peers, SortVariant<G>* v, int* per_sm) {
+  *v = sort_variant<G>(items, peers);
   cudaError_t err =
       cudaFuncSetAttribute(v->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)v->smem);
   if (err != cudaSuccess) return err;
@@ -704,12 +707,16 @@ cudaError_t scatter_variant(const LaunchOpts& o, SortVariant<G>* v, int* per_sm)
 }
 
 // The launch sequence over any geometry: histogram, plan, then per digit
-// pass (count,) scan and scatter.
+// pass (count,) scan and scatter.  Digit pass 0 (and the histogram that
+// counts for it) runs over geometry g0 with scatter variant v0, the later
+// passes over g1 with v1: each pass counts and scatters over its own ranges.
 template <class G>
-cudaError_t launch_sort_t(const G& g, uint32_t ncols, uint32_t ranges, const RangeArrays& ra,
-                          const LaunchOpts& o, const SortVariant<G>& v, cudaStream_t s,
+cudaError_t launch_sort_t(const G& g0, uint32_t ranges0, const SortVariant<G>& v0, const G& g1,
+                          uint32_t ranges1, const SortVariant<G>& v1, uint32_t ncols,
+                          const RangeArrays& ra, const LaunchOpts& o, cudaStream_t s,
                           uint32_t* launches) {
-  const unsigned count_grid = ranges * kCountCtasPerRange;
+  const G& g = g0;
+  const unsigned count_grid = ranges0 * kCountCtasPerRange;
   cudaError_t err =
       cudaMemsetAsync(ra.hist, 0, (size_t)kDigits * ra.max_ranges * kRadix * 4, s);
   if (err != cudaSuccess) return err;
@@ -732,21 +739,24 @@ cudaError_t launch_sort_t(const G& g, uint32_t ncols, uint32_t ranges, const Ran
       continue;
     }
     uint32_t* rh = ra.hist + (size_t)p * ra.max_ranges * kRadix;
+    const G& gp = p == 0 ? g0 : g1;
+    const uint32_t ranges = p == 0 ? ranges0 : ranges1;
+    const SortVariant<G>& v = p == 0 ? v0 : v1;
     record_phase(o.events, kPhasePass0 + p, false, s);
     if (p > 0) {
-      k_range_count<G><<<count_grid, kHistThreads, 0, s>>>(g, p, rh);
+      k_range_count<G><<<ranges * kCountCtasPerRange, kHistThreads, 0, s>>>(gp, p, rh);
       ++*launches;
     }
     if constexpr (std::is_same<G, OneColumn>::value) {
-      if (p == 1 && g.c.derive_ok) {  // works only in derive mode
-        k_key_starts<G><<<kKeyStartCtas, kKeyStartThreads, 0, s>>>(g);
+      if (p == 1 && gp.c.derive_ok) {  // works only in derive mode
+        k_key_starts<G><<<kKeyStartCtas, kKeyStartThreads, 0, s>>>(gp);
         ++*launches;
       }
     }
-    k_range_scan<G><<<ncols, kRangeScanThreads, 0, s>>>(g, p, rh, ra.start);
+    k_range_scan<G><<<ncols, kRangeScanThreads, 0, s>>>(gp, p, rh, ra.start);
     ++*launches;
     record_phase(o.events, kPhaseScatter0 + p, false, s);
-    v.fn<<<ranges, kSortThreads, v.smem, s>>>(g, p, ra.start);
+    v.fn<<<ranges, kSortThreads, v.smem, s>>>(gp, p, ra.start);
     ++*launches;
     record_phase(o.events, kPhaseScatter0 + p, true, s);
     record_phase(o.events, kPhasePass0 + p, true, s);
@@ -756,38 +766,47 @@ cudaError_t launch_sort_t(const G& g, uint32_t ncols, uint32_t ranges, const Ran
   return cudaSuccess;
 }
 
-cudaError_t launch_sort_one(const ColumnView& c, const RangeArrays& ra, const LaunchOpts& o,
-                            cudaStream_t s, uint32_t* launches) {
-  SortVariant<OneColumn> v;
-  int per_sm = 0;
-  cudaError_t err = scatter_variant<OneColumn>(o, &v, &per_sm);
-  if (err != cudaSuccess) return err;
-  // equal ranges of whole tiles (multiples of every tile size), one per
-  // resident scatter CTA
+// Equal ranges of whole tiles of one scatter variant (multiples of its tile
+// and of kRangeQuantum), one per resident scatter CTA.
+static OneColumn one_column_ranges(const ColumnView& c, const SortVariant<OneColumn>& v,
+                                   int per_sm, const RangeArrays& ra, const LaunchOpts& o) {
   uint64_t want = (uint64_t)std::max(o.sm_count, 1) * std::max(per_sm, 1);
   if (want > ra.max_ranges) want = ra.max_ranges;
   const uint64_t tile = (uint64_t)kSortThreads * v.items;
-  const uint64_t quantum = std::max<uint64_t>(tile, kRangeQuantum);
+  const uint64_t quantum = std::lcm<uint64_t>(tile, kRangeQuantum);
+  OneColumn g;
+  g.c = c;
+  g.range_rows = std::max<uint64_t>(ceil_div(ceil_div(c.n, want), quantum) * quantum, quantum);
+  g.ranges = (uint32_t)std::max<uint64_t>(ceil_div(c.n, g.range_rows), 1);
+  return g;
+}
+
+cudaError_t launch_sort_one(const ColumnView& c, const RangeArrays& ra, const LaunchOpts& o,
+                            cudaStream_t s, uint32_t* launches) {
+  SortVariant<OneColumn> v0, v1;
+  int per_sm0 = 0, per_sm1 = 0;
+  cudaError_t err = scatter_variant<OneColumn>(o.sort_items, o.sort_peers, &v0, &per_sm0);
+  if (err == cudaSuccess)
+    err = scatter_variant<OneColumn>(o.later_items, o.later_peers, &v1, &per_sm1);
+  if (err != cudaSuccess) return err;
   if (c.derive_ok && c.passes >= 2) {  // key counts and key starts (derive mode)
     err = cudaMemsetAsync(c.keyhist, 0, (size_t)65536 * 4, s);
     if (err == cudaSuccess) err = cudaMemsetAsync(c.keystart, 0, ceil_div(c.n, 32) * 4, s);
     if (err != cudaSuccess) return err;
   }
-  OneColumn g;
-  g.c = c;
-  g.range_rows = std::max<uint64_t>(ceil_div(ceil_div(c.n, want), quantum) * quantum, quantum);
-  g.ranges = (uint32_t)std::max<uint64_t>(ceil_div(c.n, g.range_rows), 1);
-  return launch_sort_t<OneColumn>(g, 1, g.ranges, ra, o, v, s, launches);
+  const OneColumn g0 = one_column_ranges(c, v0, per_sm0, ra, o);
+  const OneColumn g1 = one_column_ranges(c, v1, per_sm1, ra, o);
+  return launch_sort_t<OneColumn>(g0, g0.ranges, v0, g1, g1.ranges, v1, 1, ra, o, s, launches);
 }
 
 cudaError_t launch_sort_many(const ManyColumns& g, uint32_t ncols, uint32_t ranges,
                              const RangeArrays& ra, const LaunchOpts& o, cudaStream_t s,
                              uint32_t* launches) {
-  SortVariant<ManyColumns> v;
+  SortVariant<ManyColumns> v;  // one shape for every pass (the plan's ranges)
   int per_sm = 0;
-  cudaError_t err = scatter_variant<ManyColumns>(o, &v, &per_sm);
+  cudaError_t err = scatter_variant<ManyColumns>(o.sort_items, o.sort_peers, &v, &per_sm);
   if (err != cudaSuccess) return err;
-  return launch_sort_t<ManyColumns>(g, ncols, ranges, ra, o, v, s, launches);
+  return launch_sort_t<ManyColumns>(g, ranges, v, g, ranges, v, ncols, ra, o, s, launches);
 }
 
 // Copies the sorted stream from its device-chosen home into caller buffers

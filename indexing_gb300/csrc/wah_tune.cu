@@ -5,7 +5,8 @@
 // exposes them as flags (src/radix.cpp:161-184).  Here every compiled tile
 // shape of the digit passes -- rows per thread 8, 12 or 16, peer masks from
 // ballots, match.any or half of each -- is timed on a synthetic column of the
-// caller's size and bound, the fastest is applied (wah_set_tuning), and the
+// caller's size and bound, then every other shape for the passes after the
+// first one; the fastest is applied (wah_set_tuning), and the
 // choice is remembered per (device, size bucket, digit passes) in a text
 // cache file, so later processes apply it without timing.
 #include <cstdio>
@@ -131,18 +132,24 @@ int wah_autotune(uint64_t n, uint32_t bound, const char* cache_path, int* chosen
   }
   // each candidate timed over enough builds for ~20 ms, at least 2
   const int reps = n >= (1ull << 26) ? 2 : n >= (1ull << 22) ? 8 : 32;
+  // First every shape for all passes, then, with the best of those for digit
+  // pass 0, every other shape for the later passes.
   float best_ms = 0;
   int best = before;
-  for (int t : kCandidates) {
-    if (rc != WAH_OK) break;
-    if (wah_set_tuning(t) != WAH_OK) continue;
+  auto consider = [&](int t) {
+    if (rc != WAH_OK || wah_set_tuning(t) != WAH_OK) return;
     float ms = 0;
     rc = timed_build(v, n, bound, keys, offs, index, counts, ws, ws_bytes, s, a, b, reps, &ms);
     if (rc == WAH_OK && (best_ms == 0 || ms < best_ms)) {
       best_ms = ms;
       best = t;
     }
-  }
+  };
+  for (int t : kCandidates) consider(t);
+  const int first = best & 0xffff;
+  if (passes_for_bound(bound) > 1)
+    for (int t : kCandidates)
+      if (t != first) consider(first | WAH_TUNE_LATER(t));
   if (rc == WAH_OK) {
     wah_counts c{};
     e = cudaMemcpy(&c, counts, sizeof c, cudaMemcpyDeviceToHost);

@@ -149,8 +149,15 @@ def test_decoded_bitmaps_match_rows(wah):
         assert [j for j, ch in enumerate(s) if ch == "1"] == rows.tolist()
 
 
+def later(shape):
+    """WAH_TUNE_LATER: the tile shape of the digit passes after the first."""
+    return shape << 16
+
+
 @pytest.mark.parametrize("items", [8, 12, 16, 8 | 0x100, 12 | 0x100, 16 | 0x100,
-                                   8 | 0x200, 16 | 0x200])
+                                   8 | 0x200, 16 | 0x200,
+                                   16 | 0x200 | later(12 | 0x200), 16 | later(8),
+                                   8 | 0x100 | later(16 | 0x200), 12 | later(16 | 0x100)])
 def test_every_sort_tile_shape(wah, items):
     lib = wah._lib.load()
     old = lib.wah_get_tuning()
@@ -161,14 +168,20 @@ def test_every_sort_tile_shape(wah, items):
                         ("few16", 5_003)):
             v = gen(kind, n, rng)
             assert_same(wah.build_index(v), O.build(v), f"{kind}/{n}/items{items}")
+            if kind != "u32":  # two digit passes (key starts where both vary)
+                assert_same(wah.build_index(v, bound=65535), O.build(v),
+                            f"{kind}/{n}/items{items}/b16")
     finally:
         lib.wah_set_tuning(old)
 
 
 def test_rejects_unknown_tuning(wah):
-    assert wah._lib.load().wah_set_tuning(7) == wah.WAH_EINVAL
-    assert wah._lib.load().wah_set_tuning(20) == wah.WAH_EINVAL
-    assert wah._lib.load().wah_set_tuning(16 | 0x300) == wah.WAH_EINVAL
+    lib = wah._lib.load()
+    old = lib.wah_get_tuning()
+    for bad in (7, 20, 16 | 0x300, 16 | later(7), 16 | later(12 | 0x300), 16 | later(0x200),
+                -1):
+        assert lib.wah_set_tuning(bad) == wah.WAH_EINVAL, bad
+    assert lib.wah_get_tuning() == old
 
 
 def test_pipeline_matches_oracle(wah):
