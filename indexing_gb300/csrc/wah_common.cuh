@@ -31,7 +31,7 @@ constexpr int kMaxRanges = 1024;
 constexpr int kCountCtasPerRange = 2;
 
 
-// Fused index build: 256 threads x 8 rows, blocked.
+// Fused index build: 128 threads x 16 rows, blocked.
 constexpr int kBuildThreads = 128;
 constexpr int kBuildItems = 16;
 constexpr int kBuildTile = kBuildThreads * kBuildItems;  // 2048 rows

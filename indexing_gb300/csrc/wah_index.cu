@@ -20,16 +20,21 @@
 //   k_build_count  streams the range's rows (128-bit loads) and counts its
 //                  words, keys and segments
 //   k_build_scan   exclusive scan over ranges: each range's first word and key
-//   k_build_emit   one persistent CTA per range walks its tiles of 2048 rows;
-//                  the next tile's window (4 rows behind, 32 ahead: a segment
-//                  has at most 31 rows, so the tile owning a segment's head
-//                  can finish its literal) is fetched by cp.async.bulk while
-//                  this one is processed; literals come from a reverse
-//                  segmented OR over each thread's 8 rows; a block scan gives
-//                  tile-local positions; words, keys and offsets are staged in
-//                  shared memory and written once, coalesced, at the range's
-//                  running offsets.  No zero word is ever written and no
-//                  compaction pass is needed.
+//   k_build_emit   one persistent CTA per range (128 threads x 16 rows) walks
+//                  its tiles of 2048 rows; the next tile's window (4 rows
+//                  behind, 32 ahead: a segment has at most 31 rows, so the
+//                  tile owning a segment's head can finish its literal) is
+//                  fetched by cp.async.bulk while this one is processed;
+//                  literals come from a reverse segmented OR over each
+//                  thread's rows; a block scan gives tile-local positions;
+//                  words are staged in the tile's own window buffer, keys and
+//                  offsets beside it, and written once, coalesced, at the
+//                  range's running offsets.  No zero word is ever written and
+//                  no compaction pass is needed.
+// In key-start mode (the sort's plan: every key below 2^16, both low digits
+// vary) the sorted keys are never written; the count and the emit read the
+// row ids and one key-start bit per row instead, and the keys come from the
+// sort's key counts.
 #include <algorithm>
 #include <type_traits>
 

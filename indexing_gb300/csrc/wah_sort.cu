@@ -15,7 +15,10 @@
 //   k_sort_plan        trivial digits (every key shares them) skipped, homes
 //                      of each pass
 //   k_range_count      for digit passes after the first: per-range histogram
-//                      of the digit over the current order (one read of keys)
+//                      of the digit over the current order (one read of keys);
+//                      in key-start mode also the rows of every 16-bit key
+//   k_key_starts       key-start mode: the first row of every key in the
+//                      sorted order marked in a bit per row, the keys written
 //   k_range_scan       start of every (range, bin) = bin offset (a scan of
 //                      the bins' totals over all ranges) + counts of the same
 //                      bin in earlier ranges
@@ -24,7 +27,11 @@
 //                      while this one is ranked (warp peer masks, stable per
 //                      warp counters), staged in tile-sorted order and written
 //                      out run by run at the range's running bin offsets.  The
-//                      first active pass takes rid = row index.
+//                      first active pass takes rid = row index.  Digit pass 0
+//                      and the later passes may use different tile shapes,
+//                      each over its own ranges; keys between two passes are
+//                      16-bit when every key is below 2^16, and in key-start
+//                      mode the last pass writes row ids only.
 #include <algorithm>
 #include <numeric>
 #include <type_traits>
