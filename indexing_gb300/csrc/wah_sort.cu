@@ -722,17 +722,16 @@ cudaError_t launch_sort_t(const G& g0, uint32_t ranges0, const SortVariant<G>& v
                           uint32_t ranges1, const SortVariant<G>& v1, uint32_t ncols,
                           const RangeArrays& ra, const LaunchOpts& o, cudaStream_t s,
                           uint32_t* launches) {
-  const G& g = g0;
   const unsigned count_grid = ranges0 * kCountCtasPerRange;
   cudaError_t err =
       cudaMemsetAsync(ra.hist, 0, (size_t)kDigits * ra.max_ranges * kRadix * 4, s);
   if (err != cudaSuccess) return err;
   record_phase(o.events, kPhaseHist, false, s);
-  k_digit_histogram<G><<<count_grid, kHistThreads, 0, s>>>(g, ra.hist);
+  k_digit_histogram<G><<<count_grid, kHistThreads, 0, s>>>(g0, ra.hist);
   record_phase(o.events, kPhaseHist, true, s);
   ++*launches;
   record_phase(o.events, kPhasePlan, false, s);
-  k_sort_plan<G><<<ncols, kRadix, 0, s>>>(g);
+  k_sort_plan<G><<<ncols, kRadix, 0, s>>>(g0);
   record_phase(o.events, kPhasePlan, true, s);
   ++*launches;
   err = cudaGetLastError();
