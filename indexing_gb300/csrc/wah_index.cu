@@ -52,11 +52,6 @@ __device__ __forceinline__ uint32_t skew(uint32_t i) { return i + (i >> 5); }
 constexpr int kSkewed(int n) { return n + n / 32 + 1; }
 constexpr int kStagedWords = kSkewed(2 * kBuildTile);  // a tile's words, skewed
 
-__device__ __forceinline__ uint32_t chunk_bit(uint32_t rid) {
-  const uint32_t c = rid / 31;
-  return (c << 5) | (rid - c * 31);
-}
-
 // A tile's words (<= 2 per row) and keys (<= 1 per row) pack into one
 // 32-bit scan value: words in the low 16 bits, keys in the high 16.
 constexpr int kPackShift = 16;
@@ -368,17 +363,19 @@ __device__ __forceinline__ void build_emit(const G& g, const uint32_t* __restric
 
     // This thread's rows from the window (16-byte loads).
     static_assert(kBuildItems % 4 == 0, "whole 16-byte loads");
-    uint32_t v[kBuildItems], cb[kBuildItems];
+    uint32_t v[kBuildItems], ch[kBuildItems], bt[kBuildItems];  // key, chunk, bit in chunk
     {
       const uint4* r4 = reinterpret_cast<const uint4*>(wr + kWinBehind + first);
       const uint4* v4 = reinterpret_cast<const uint4*>(wv + kWinBehind + first);
 #pragma unroll
       for (int q = 0; q < kBuildItems / 4; ++q) {
         const uint4 b = r4[q];
-        cb[4 * q + 0] = chunk_bit(b.x);
-        cb[4 * q + 1] = chunk_bit(b.y);
-        cb[4 * q + 2] = chunk_bit(b.z);
-        cb[4 * q + 3] = chunk_bit(b.w);
+        const uint32_t r[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          ch[4 * q + i] = r[i] / 31;
+          bt[4 * q + i] = r[i] - ch[4 * q + i] * 31;
+        }
         if (!derive) {
           const uint4 a = v4[q];
           v[4 * q + 0] = a.x; v[4 * q + 1] = a.y; v[4 * q + 2] = a.z; v[4 * q + 3] = a.w;
@@ -410,7 +407,7 @@ __device__ __forceinline__ void build_emit(const G& g, const uint32_t* __restric
     uint32_t nw = 0;
 #pragma unroll
     for (int j = 0; j < kBuildItems; ++j) {
-      const uint32_t c = cb[j] >> 5;
+      const uint32_t c = ch[j];
       const bool ok = full || first + j < valid;
       const bool vh = derive ? ((kbits >> j) & 1u) != 0 : v[j] != pv;
       // x as in count_words: 0 continues the segment, else the fill is x - 1
@@ -430,7 +427,7 @@ __device__ __forceinline__ void build_emit(const G& g, const uint32_t* __restric
     // segment (from the window), then a reverse segmented OR over its rows.
     uint32_t acc = 0;
     {
-      const uint32_t v7 = v[kBuildItems - 1], c7 = cb[kBuildItems - 1] >> 5;
+      const uint32_t v7 = v[kBuildItems - 1], c7 = ch[kBuildItems - 1];
       for (uint32_t m = first + kBuildItems; m < wend; ++m) {
         const uint32_t rm = wr[kWinBehind + m];
         if (rm / 31 != c7) break;
@@ -445,7 +442,7 @@ __device__ __forceinline__ void build_emit(const G& g, const uint32_t* __restric
     uint32_t lits[kBuildItems];
 #pragma unroll
     for (int j = kBuildItems - 1; j >= 0; --j) {
-      if (first + j < exist) acc |= 1u << (cb[j] & 31);  // rows past n add nothing
+      if (first + j < exist) acc |= 1u << bt[j];  // rows past n add nothing
       lits[j] = acc | 0x80000000u;
       if (headm & (1u << j)) acc = 0;
     }
