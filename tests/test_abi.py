@@ -60,3 +60,22 @@ def test_rejects_oversize_without_touching_device(lib):
     # n >= 2^30 is refused before any CUDA call
     rc = lib.wah_build(None, 1 << 30, 0, None, None, None, ctypes.c_void_p(16), None, 0, None)
     assert rc == 5
+
+
+def test_tuning_encoding(lib):
+    # host-only: the tile shape of digit pass 0 in the low 16 bits, that of
+    # the later passes in the high 16 (0: the same); bad shapes are refused
+    # and leave the tuning unchanged
+    old = lib.wah_get_tuning()
+    try:
+        for good in (8, 12, 16, 16 | 0x100, 12 | 0x200, (16 | 0x200) | ((12 | 0x200) << 16),
+                     8 | (16 << 16)):
+            assert lib.wah_set_tuning(good) == 0, good
+            assert lib.wah_get_tuning() == good
+        cur = lib.wah_get_tuning()
+        for bad in (0, 7, 20, 16 | 0x300, 16 | 0x400, 16 | (7 << 16), 16 | (0x200 << 16),
+                    16 | ((12 | 0x300) << 16), -1):
+            assert lib.wah_set_tuning(bad) == 1, bad  # WAH_EINVAL
+            assert lib.wah_get_tuning() == cur
+    finally:
+        lib.wah_set_tuning(old)
