@@ -425,7 +425,7 @@ __device__ __forceinline__ void build_emit(const G& g, const uint32_t* __restric
 
     // Literals: the rows after this thread's last row that continue its last
     // segment (from the window), then a reverse segmented OR over its rows.
-    uint32_t acc = 0;
+    uint32_t acc = 0x80000000u;  // the literal flag, set from the start
     {
       const uint32_t v7 = v[kBuildItems - 1], c7 = ch[kBuildItems - 1];
       for (uint32_t m = first + kBuildItems; m < wend; ++m) {
@@ -443,8 +443,8 @@ __device__ __forceinline__ void build_emit(const G& g, const uint32_t* __restric
 #pragma unroll
     for (int j = kBuildItems - 1; j >= 0; --j) {
       if (first + j < exist) acc |= 1u << bt[j];  // rows past n add nothing
-      lits[j] = acc | 0x80000000u;
-      if (headm & (1u << j)) acc = 0;
+      lits[j] = acc;
+      if (headm & (1u << j)) acc = 0x80000000u;
     }
 
     // Tile scan of (words, keys); the warp totals are read before the
