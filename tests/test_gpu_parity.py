@@ -108,6 +108,18 @@ def test_sort_phase_matches_stable_sort(wah):
         assert np.array_equal(sr.cpu().numpy().view(np.uint32), er)
 
 
+def test_sort_phase_with_bound(wah):
+    # two digit passes with 16-bit keys between them: the sort alone still
+    # returns every sorted key (key starts are an index-build mode only)
+    rng = np.random.default_rng(31)
+    for n, m in ((4097, 65536), (300_000, 65536), (1 << 20, 40_000), (77_777, 300)):
+        v = rng.integers(0, m, size=n, dtype=np.uint32)
+        sv, sr = wah.sort_rids_by_value(v, bound=65535)
+        ev, er = O.sort_rids_by_value(v)
+        assert np.array_equal(sv.cpu().numpy().view(np.uint32), ev), (n, m)
+        assert np.array_equal(sr.cpu().numpy().view(np.uint32), er), (n, m)
+
+
 def test_build_sorted_phase(wah):
     rng = np.random.default_rng(4)
     v = rng.integers(0, 1000, size=123_457, dtype=np.uint32)
