@@ -395,9 +395,11 @@ uint32_t wah_last_launch_count(void);
  * 256 threads per tile), optionally OR WAH_TUNE_MATCH to build the digit
  * peer masks with match.any instead of ballots, or WAH_TUNE_HYBRID to build
  * 3/8 of them with match.any and the rest with ballots.  That shape applies
- * to digit pass 0; WAH_TUNE_LATER(shape) ORed in gives one-column builds a
+ * to digit pass 0; WAH_TUNE_LATER(shape) ORed in gives one-column index
+ * builds (wah_build and its host-buffer forms; not the sort alone) a
  * different shape for the later passes (0: the same).  Process-wide; set by
- * the autotuner or the caller before builds are enqueued.  The reference
+ * the autotuner or the caller before builds are enqueued; the default is
+ * 16 | WAH_TUNE_HYBRID | WAH_TUNE_LATER(12 | WAH_TUNE_HYBRID).  The reference
  * hard-codes its radix shape (src/phases.cpp:445-453). */
 #define WAH_TUNE_MATCH 0x100
 #define WAH_TUNE_HYBRID 0x200

@@ -15,8 +15,12 @@ namespace wah {
 
 thread_local uint32_t g_last_launches = 0;
 // Tile shape of the digit passes (wah_set_tuning): rows per thread | peer
-// mode flags, one atomic word so concurrent builds read a consistent pair.
-std::atomic<int> g_tuning{16};
+// mode flags, for digit pass 0 and (upper 16 bits) the later passes, one
+// atomic word so concurrent builds read a consistent set.  The default is
+// the autotuner's choice on GB300 for a 268M-row 16-bit column: 16 rows per
+// thread for pass 0, 12 for the later passes, 3/8 of the peer masks by
+// match.any in both.
+std::atomic<int> g_tuning{(16 | WAH_TUNE_HYBRID) | WAH_TUNE_LATER(12 | WAH_TUNE_HYBRID)};
 
 uint32_t* last_launches_slot() { return &g_last_launches; }
 

@@ -379,7 +379,7 @@ struct RangeArrays {
 struct LaunchOpts {
   int sort_items;       // radix tile rows per thread (8, 12, 16) of digit pass 0
   int sort_peers;       // peer masks: 0 ballots, 1 match.any, 2 half and half
-  int later_items;      // the same for the later digit passes (one-column builds)
+  int later_items;      // the same for the later digit passes (one-column index builds)
   int later_peers;
   int max_passes;       // digit passes launched (max over the columns)
   int sm_count;

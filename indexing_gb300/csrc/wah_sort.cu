@@ -791,9 +791,13 @@ cudaError_t launch_sort_one(const ColumnView& c, const RangeArrays& ra, const La
                             cudaStream_t s, uint32_t* launches) {
   SortVariant<OneColumn> v0, v1;
   int per_sm0 = 0, per_sm1 = 0;
+  // The later passes' own shape is for index builds, whose last pass writes
+  // row ids only (key-start mode); a sort returns its keys and keeps one shape.
   cudaError_t err = scatter_variant<OneColumn>(o.sort_items, o.sort_peers, &v0, &per_sm0);
   if (err == cudaSuccess)
-    err = scatter_variant<OneColumn>(o.later_items, o.later_peers, &v1, &per_sm1);
+    err = c.derive_ok
+              ? scatter_variant<OneColumn>(o.later_items, o.later_peers, &v1, &per_sm1)
+              : scatter_variant<OneColumn>(o.sort_items, o.sort_peers, &v1, &per_sm1);
   if (err != cudaSuccess) return err;
   if (c.derive_ok && c.passes >= 2) {  // key counts and key starts (derive mode)
     err = cudaMemsetAsync(c.keyhist, 0, (size_t)65536 * 4, s);
