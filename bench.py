@@ -18,6 +18,10 @@ SHOW_TIME_CONSUMPTION output, src/phases.cpp:714-1127) go to stderr.
               keys/offsets/index, every step; consecutive steps overlap
   roofline    the dominant kernel's algorithmic bytes / its mean event-timed
               duration, against the measured HBM copy bandwidth
+  column_roofline  the whole build on the scope table's byte formula
+              (40n + 24k + 4L + 8K) over the build time, same peak
+  autotune    the radix tile shapes timed and applied before the run (digit
+              pass 0's shape, and the later passes' in the upper 16 bits)
   cpu_baseline  the oracle (plain-C restatement of the reference `cpu`
               program) on a bounded sample, host cores of this machine
   decode      the built index decoded back to row ids on the device, and
