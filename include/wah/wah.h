@@ -413,7 +413,8 @@ int wah_get_tuning(void);
  * fixed, src/phases.cpp:445-453; its radix test program takes it as flags,
  * src/radix.cpp:161-184), applies the fastest, and appends it to the text
  * file cache_path (NULL: no cache) under the key (device name, floor(log2 n),
- * digit passes).  When the cache already holds the key, its entry is applied
+ * digit passes, format tag "t2" for entries that carry the later passes'
+ * shape).  When the cache already holds the key, its entry is applied
  * without timing and *from_cache is 1.  Allocates and frees its own device
  * memory; synchronises.  *chosen receives the tuning applied.
  */

@@ -47,7 +47,9 @@ std::string cache_key(int device, uint64_t n, uint32_t bound) {
     if (c == ' ' || c == '\t') c = '_';
   int bucket = 0;
   while (bucket < 63 && (2ull << bucket) <= n) ++bucket;  // floor(log2 n)
-  return name + " " + std::to_string(bucket) + " " + std::to_string(passes_for_bound(bound));
+  // "t2": entries that hold a later-pass shape (older entries are timed again)
+  return name + " " + std::to_string(bucket) + " " + std::to_string(passes_for_bound(bound)) +
+         " t2";
 }
 
 bool cache_lookup(const char* path, const std::string& key, int* tuning) {
