@@ -408,10 +408,11 @@ int wah_set_tuning(int sort_items);
 int wah_get_tuning(void);
 
 /*
- * Autotuner: times every tile shape wah_set_tuning accepts on a synthetic
- * column of n rows with values up to bound (the reference's radix shape is
- * fixed, src/phases.cpp:445-453; its radix test program takes it as flags,
- * src/radix.cpp:161-184), applies the fastest, and appends it to the text
+ * Autotuner: times every tile shape for all digit passes, then every other
+ * shape for the passes after the first (WAH_TUNE_LATER), by index builds of
+ * a synthetic column of n rows with values up to bound (the reference's
+ * radix shape is fixed, src/phases.cpp:445-453; its radix test program takes
+ * it as flags, src/radix.cpp:161-184), applies the fastest, and appends it to the text
  * file cache_path (NULL: no cache) under the key (device name, floor(log2 n),
  * digit passes, format tag "t2" for entries that carry the later passes'
  * shape).  When the cache already holds the key, its entry is applied
