@@ -101,10 +101,13 @@ int wah_build(const uint32_t* d_values, uint64_t n, uint32_t bound,
  * build's scratch memory is a fixed array in the library's device image
  * (22 MiB, held by every GPU that loads the library until exit).  Columns of
  * up to WAH_NOALLOC_MAX_ROWS rows; larger n returns WAH_ERANGE without
- * enqueueing anything.  Calls no allocator.  All calls share the array:
+ * enqueueing anything (d_counts is left untouched then, so it does not hold
+ * this call's result).  Calls no allocator.  All calls share the array:
  * calls whose work overlaps on the GPU (unordered streams or host threads)
- * race.  The first call on a device looks up the array's device address with
- * that device current; make it before any stream capture on the device.
+ * race.  The array has its own address in every CUDA context (primary or
+ * created by the caller); each call looks it up in the context current on
+ * the calling thread.  The first call in a context may load the library's
+ * device code there; make it before any stream capture.
  */
 #define WAH_NOALLOC_MAX_ROWS ((uint64_t)1 << 20)
 int wah_build_noalloc(const uint32_t* d_values, uint64_t n, uint32_t bound,

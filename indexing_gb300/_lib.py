@@ -33,31 +33,42 @@ def nvcc() -> str:
     return "nvcc"
 
 
-def build(verbose: bool = False) -> str:
-    """Compile every CUDA source (in parallel) and link libwah_gb300.so."""
+def build(verbose: bool = False, force: bool = False, report=None) -> str:
+    """Compile every CUDA source (in parallel) and link libwah_gb300.so.
+
+    Without ``force`` an object newer than its source and every header is
+    reused; ``force=True`` compiles every source and relinks whatever is on
+    disk (a copied tree can carry objects built elsewhere).  ``report``, a
+    list, receives the sources compiled and whether the library was linked.
+    """
     os.makedirs(OBJ_DIR, exist_ok=True)
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
     headers.append(os.path.join(INCLUDE, "wah", "wah.h"))
     newest_header = max(os.path.getmtime(h) for h in headers)
 
-    def compile_one(src: str) -> str:
+    def compile_one(src: str):
         obj = os.path.join(OBJ_DIR, src.replace(".cu", ".o"))
         path = os.path.join(CSRC, src)
-        if (os.path.exists(obj) and os.path.getmtime(obj) >= os.path.getmtime(path)
+        if (not force and os.path.exists(obj) and os.path.getmtime(obj) >= os.path.getmtime(path)
                 and os.path.getmtime(obj) >= newest_header):
-            return obj
+            return obj, False
         cmd = [nvcc(), *NVCC_FLAGS, "-c", path, "-o", obj]
         if verbose:
             cmd.insert(1, "-Xptxas=-v")
         subprocess.run(cmd, check=True)
-        return obj
+        return obj, True
 
     with ThreadPoolExecutor(max_workers=len(CUDA_SOURCES)) as ex:
-        objs = list(ex.map(compile_one, CUDA_SOURCES))
-    if (not os.path.exists(LIB_PATH)
-            or any(os.path.getmtime(o) > os.path.getmtime(LIB_PATH) for o in objs)):
+        done = list(ex.map(compile_one, CUDA_SOURCES))
+    objs = [o for o, _ in done]
+    linked = (force or not os.path.exists(LIB_PATH)
+              or any(os.path.getmtime(o) > os.path.getmtime(LIB_PATH) for o in objs))
+    if linked:
         subprocess.run([nvcc(), "-gencode", "arch=compute_103a,code=sm_103a", "-shared",
                         *objs, "-o", LIB_PATH], check=True)
+    if report is not None:
+        report.extend(src for src, (_, built) in zip(CUDA_SOURCES, done) if built)
+        report.append(("linked", linked))
     return LIB_PATH
 
 
@@ -65,17 +76,18 @@ HOST_DIR = os.path.join(PKG_DIR, "host")
 BIN_DIR = os.path.join(PKG_DIR, "bin")
 # host programs: (source, links libwah_gb300.so)
 HOST_PROGRAMS = [("phases.cpp", True), ("gpu.cpp", True), ("overhead.cpp", True),
-                 ("generate.cpp", False), ("actors_test.cpp", False)]
+                 ("generate.cpp", False)]
 CXX_FLAGS = ["-O2", "-std=c++17", "-pthread", "-Wall", "-Wextra", "-I" + INCLUDE]
 
 
-def build_host(names=None) -> dict:
+def build_host(names=None, force: bool = False) -> dict:
     """Compile the C++ host programs into indexing_gb300/bin/ with g++.
 
-    phases and gpu link libwah_gb300.so (found next to the package through an
-    $ORIGIN rpath); generate and actors_test need no GPU library.  `names`
-    limits the build to some programs (e.g. ["actors_test", "generate"]).  Plain g++
-    without -march flags, so the same recipe builds on x86-64 and aarch64.
+    phases, gpu and overhead link libwah_gb300.so (found next to the package
+    through an $ORIGIN rpath); generate needs no GPU library.  `names` limits
+    the build to some programs (e.g. ["generate"]); ``force`` recompiles
+    programs that look up to date.  Plain g++ without -march flags, so the
+    same recipe builds on x86-64 and aarch64.
     """
     os.makedirs(BIN_DIR, exist_ok=True)
     headers = [os.path.join(HOST_DIR, f) for f in os.listdir(HOST_DIR) if f.endswith(".hpp")]
@@ -90,7 +102,7 @@ def build_host(names=None) -> dict:
         deps = [os.path.getmtime(path), newest_header]
         if link:
             deps.append(os.path.getmtime(LIB_PATH))
-        if os.path.exists(out) and all(os.path.getmtime(out) >= t for t in deps):
+        if not force and os.path.exists(out) and all(os.path.getmtime(out) >= t for t in deps):
             return out
         cmd = [cxx, *CXX_FLAGS, path, "-o", out]
         if link:

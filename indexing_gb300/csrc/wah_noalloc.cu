@@ -13,16 +13,20 @@
 // The array is a file-scope __device__ variable of kNoAllocBytes, so every
 // GPU that loads the library holds it until the process exits.  Columns of up
 // to WAH_NOALLOC_MAX_ROWS rows fit; longer ones are refused with WAH_ERANGE
-// before anything is enqueued.  All calls share the array and it keeps the
-// last call's contents: the build clears everything it needs zeroed itself,
-// but two calls whose work overlaps on the GPU (different streams, or
-// different host threads, without ordering between them) race on it.
+// before anything is enqueued (d_counts is then left untouched).  All calls
+// share the array and it keeps the last call's contents: the build clears
+// everything it needs zeroed itself, but two calls whose work overlaps on the
+// GPU (different streams, or different host threads, without ordering
+// between them) race on it.
 //
-// The device address of the array is looked up once per device, with that
-// device current, by the first call on it (cudaGetSymbolAddress); make that
-// first call before any stream capture on the device.
-#include <mutex>
-
+// The array has its own device address in every CUDA context that loads the
+// library (the primary context of each device, a context the caller created
+// with the driver API, a context re-created after cudaDeviceReset).  So every
+// call looks the address up again in the context current on the calling
+// thread (cudaGetSymbolAddress: a host-side table lookup once the module is
+// loaded, no allocation and no device work); nothing is cached across calls.
+// The first call in a context loads the library's device code into it when
+// loading is lazy: make that first call before any stream capture.
 #include "wah_common.cuh"
 
 namespace {
@@ -32,24 +36,15 @@ constexpr size_t kNoAllocBytes = (size_t)22 << 20;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
-constexpr int kMaxDevices = 64;
-std::mutex g_noalloc_mu;
-void* g_noalloc_ptr[kMaxDevices] = {};
-
-// Device address of g_noalloc_scratch on the current device (set-up on first
-// use per device).  Host code cannot pass the symbol itself: on the host it is
-// only a stand-in, not a device address.
+// Device address of g_noalloc_scratch in the current context.  Host code
+// cannot pass the symbol itself: on the host it is only a stand-in, not a
+// device address.
 int noalloc_scratch(void** out) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return WAH_ENODEV;
-  if (dev < 0 || dev >= kMaxDevices) return WAH_ENODEV;
-  std::lock_guard<std::mutex> lock(g_noalloc_mu);
-  if (!g_noalloc_ptr[dev]) {
-    void* p = nullptr;
-    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return WAH_ECUDA;
-    g_noalloc_ptr[dev] = p;
-  }
-  *out = g_noalloc_ptr[dev];
+  void* p = nullptr;
+  if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return WAH_ECUDA;
+  *out = p;
   return WAH_OK;
 }
 

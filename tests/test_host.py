@@ -15,8 +15,14 @@ ORACLE_DIR = os.path.join(REPO, "oracle")
 
 
 @pytest.fixture(scope="module")
-def progs():
-    return _lib.build_host(["actors_test", "generate"])
+def progs(tmp_path_factory):
+    progs = _lib.build_host(["generate"])
+    exe = tmp_path_factory.mktemp("native") / "actors_test"
+    subprocess.run(["g++", "-O2", "-std=c++17", "-pthread", "-Wall", "-Wextra",
+                    "-I" + _lib.HOST_DIR, os.path.join(REPO, "tests", "native", "actors_test.cpp"),
+                    "-o", str(exe)], check=True)
+    progs["actors_test"] = str(exe)
+    return progs
 
 
 @pytest.fixture(scope="module")

@@ -37,7 +37,7 @@ def san_dir(tmp_path_factory):
 def test_actor_runtime_sanitized(san_dir):
     exe = san_dir / "actors_test"
     subprocess.run(["g++", "-std=c++17", "-pthread", *SAN, "-I" + _lib.HOST_DIR,
-                    os.path.join(_lib.HOST_DIR, "actors_test.cpp"), "-o", str(exe)], check=True)
+                    os.path.join(REPO, "tests", "native", "actors_test.cpp"), "-o", str(exe)], check=True)
     r = subprocess.run([str(exe)], capture_output=True, text=True, env=ENV, timeout=300)
     assert r.returncode == 0, r.stderr[-2000:]
     assert "all checks passed" in r.stdout
