@@ -87,16 +87,23 @@ def parse():
     ap.add_argument("--no-decode", action="store_true")
     ap.add_argument("--no-append", action="store_true")
     ap.add_argument("--no-c1", action="store_true")
+    ap.add_argument("--no-link", action="store_true", help="skip the copy-only host-link leg")
+    ap.add_argument("--no-cub", action="store_true", help="skip the CUB sort speed reference")
     ap.add_argument("--serve-requests", type=int, default=20000)
     ap.add_argument("--serve-budget-gb", type=int, default=64)
     ap.add_argument("--pipe-depth", type=int, default=3,
                     help="builds in flight in the end-to-end leg")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-parity", action="store_true",
+                    help="skip the oracle checks of the C2, C3, C4 and C5 results (run after "
+                         "every timed leg)")
     ap.add_argument("--sort-items", type=int, default=0,
                     help="radix scatter tuning: rows per thread | peer-mask flags, optionally "
                          "| (later passes' shape << 16) (0: library default)")
     ap.add_argument("--cpu-sample", type=int, default=1 << 23,
-                    help="rows per oracle build in the CPU legs")
+                    help="rows per oracle build in the CPU-baseline leg")
+    ap.add_argument("--ref-sample", type=int, default=1 << 25,
+                    help="rows per step of --impl reference (a slice of the same column)")
     return ap.parse_args()
 
 
@@ -222,8 +229,10 @@ def gen_skewed(kind: str, n: int, seed: int, torch, dev):
     raise ValueError(kind)
 
 
-def bench_skewed(args, lib, wah, torch, dev, stream):
-    """C3: skewed and clustered single columns of args.n rows, bound 65535."""
+def bench_skewed(args, lib, wah, torch, dev, stream, keep=None):
+    """C3: skewed and clustered single columns of args.n rows, bound 65535.
+    keep (a list) receives (kind, host values, host result) of each column
+    for the oracle check after every timed leg."""
     out = {}
     for kind in ("zipf1.1", "distinct16", "runs1000"):
         v = gen_skewed(kind, args.n, args.seed, torch, dev)
@@ -241,24 +250,198 @@ def bench_skewed(args, lib, wah, torch, dev, stream):
         assert c[3] == 0
         out[kind] = {"rows_per_s": args.n / (ms / 1e3), "ms": ms, "keycnt": int(c[0]),
                      "index_len": int(c[1]), "merged": int(c[2])}
+        if keep is not None:
+            keep.append((kind, v.cpu().numpy().view(np.uint32),
+                         result_numpy(bufs.keys, bufs.offsets, bufs.index, bufs.counts)))
         del v, bufs
         torch.cuda.empty_cache()
     return out
 
 
-def bench_batched(args, lib, wah, torch, dev, stream):
+def _cpulist(ids) -> str:
+    ids = sorted(ids)
+    out, i = [], 0
+    while i < len(ids):
+        j = i
+        while j + 1 < len(ids) and ids[j + 1] == ids[j] + 1:
+            j += 1
+        out.append(str(ids[i]) if i == j else f"{ids[i]}-{ids[j]}")
+        i = j + 1
+    return ",".join(out)
+
+
+def numa_info(torch, dev, host_ptr=None) -> dict:
+    """Where the GPU, this process's CPUs and a pinned host buffer sit
+    (sysfs and /proc/self/numa_maps; best effort, None where unknown)."""
+    import glob
+    info = {"gpu_numa_node": None, "nodes": {}, "process_cpus": None, "buffer_pages_by_node": None}
+    try:
+        p = torch.cuda.get_device_properties(dev)
+        bus = f"{p.pci_domain_id:04x}:{p.pci_bus_id:02x}:{p.pci_device_id:02x}.0"
+        with open(f"/sys/bus/pci/devices/{bus}/numa_node") as f:
+            info["gpu_numa_node"] = int(f.read())
+        info["gpu_pci"] = bus
+    except Exception:
+        pass
+    for d in sorted(glob.glob("/sys/devices/system/node/node[0-9]*")):
+        node = int(d.rsplit("node", 1)[1])
+        entry = {}
+        try:
+            with open(d + "/cpulist") as f:
+                entry["cpus"] = f.read().strip()
+            with open(d + "/meminfo") as f:
+                for line in f:
+                    if "MemTotal" in line:
+                        entry["mem_gb"] = round(int(line.split()[-2]) / 2**20, 1)
+        except OSError:
+            pass
+        info["nodes"][node] = entry
+    try:
+        info["process_cpus"] = _cpulist(os.sched_getaffinity(0))
+    except Exception:
+        pass
+    if host_ptr:
+        try:
+            start = None
+            with open("/proc/self/maps") as f:
+                for line in f:
+                    a, b = (int(x, 16) for x in line.split()[0].split("-"))
+                    if a <= host_ptr < b:
+                        start = a
+                        break
+            with open("/proc/self/numa_maps") as f:
+                for line in f:
+                    parts = line.split()
+                    if start is not None and int(parts[0], 16) == start:
+                        info["buffer_pages_by_node"] = {
+                            x.split("=")[0]: int(x.split("=")[1]) for x in parts
+                            if x.startswith("N") and "=" in x}
+                        info["buffer_policy"] = parts[1]
+        except Exception:
+            pass
+    return info
+
+
+def bench_link(torch, dev, h2d_bytes: int, d2h_bytes: int, reps: int = 5):
+    """Copy-only leg with the end-to-end step's bytes: pinned host ->
+    device alone, device -> pinned host alone, and both at once on two
+    streams (CUDA events); the last is the host-link floor of one step."""
+    hb = torch.empty(max(h2d_bytes, d2h_bytes), dtype=torch.uint8, pin_memory=True)
+    hb2 = torch.empty(d2h_bytes, dtype=torch.uint8, pin_memory=True)
+    db = torch.empty(max(h2d_bytes, d2h_bytes), dtype=torch.uint8, device=dev)
+    db2 = torch.empty(d2h_bytes, dtype=torch.uint8, device=dev)
+    s1, s2 = torch.cuda.Stream(dev), torch.cuda.Stream(dev)
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        cur = torch.cuda.current_stream(dev)
+        a.record(cur)
+        s1.wait_stream(cur)
+        s2.wait_stream(cur)
+        for _ in range(reps):
+            fn()
+        cur.wait_stream(s1)
+        cur.wait_stream(s2)
+        b.record(cur)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b) / reps
+
+    def h2d():
+        with torch.cuda.stream(s1):
+            db[:h2d_bytes].copy_(hb[:h2d_bytes], non_blocking=True)
+
+    def d2h():
+        with torch.cuda.stream(s2):
+            hb2.copy_(db2, non_blocking=True)
+
+    def both():
+        h2d()
+        d2h()
+    ms_h2d, ms_d2h, ms_both = timed(h2d), timed(d2h), timed(both)
+    out = {"h2d_bytes": h2d_bytes, "d2h_bytes": d2h_bytes,
+           "h2d_gbs": h2d_bytes / ms_h2d / 1e6, "d2h_gbs": d2h_bytes / ms_d2h / 1e6,
+           "both_ms": ms_both, "both_gbs": (h2d_bytes + d2h_bytes) / ms_both / 1e6,
+           "numa": numa_info(torch, dev, hb.data_ptr())}
+    del hb, hb2, db, db2
+    torch.cuda.empty_cache()
+    return out
+
+
+def bench_cub_sort(torch, dev, d_values, n: int, reps: int = 3):
+    """External speed reference for the sort phase: CUB's DeviceRadixSort
+    SortPairs of (value, row id) over the same column, (a) 32-bit keys
+    sorted on bits [0, 16) and (b) the keys as 16-bit integers, all bits; two
+    8-bit digit passes each (CUB's onesweep).  Event-timed, inputs resident."""
+    import ctypes as C
+    from indexing_gb300 import _lib
+    if not os.path.exists(_lib.SPEEDREF_PATH):
+        return None
+    lib = C.CDLL(_lib.SPEEDREF_PATH)
+    lib.speedref_sort_pairs_u32_bytes.restype = C.c_size_t
+    lib.speedref_sort_pairs_u32_bytes.argtypes = [C.c_uint64]
+    lib.speedref_sort_pairs_u16_bytes.restype = C.c_size_t
+    lib.speedref_sort_pairs_u16_bytes.argtypes = [C.c_uint64]
+    vp = C.c_void_p
+    lib.speedref_sort_pairs_u32.argtypes = [vp, vp, vp, vp, C.c_uint64, C.c_int, C.c_int, vp,
+                                            C.c_size_t, vp]
+    lib.speedref_sort_pairs_u16.argtypes = [vp, vp, vp, vp, C.c_uint64, vp, C.c_size_t, vp]
+    stream = torch.cuda.current_stream(dev)
+    sh = stream.cuda_stream
+    rids = torch.arange(n, dtype=torch.int32, device=dev)
+    vals_out = torch.empty(n, dtype=torch.int32, device=dev)
+    out = {}
+    tb = int(lib.speedref_sort_pairs_u32_bytes(n))
+    temp = torch.empty(tb, dtype=torch.uint8, device=dev)
+    keys_out = torch.empty(n, dtype=torch.int32, device=dev)
+
+    def s32():
+        assert lib.speedref_sort_pairs_u32(d_values.data_ptr(), keys_out.data_ptr(),
+                                           rids.data_ptr(), vals_out.data_ptr(), n, 0, 16,
+                                           temp.data_ptr(), tb, sh) == 0
+    s32()
+    out["u32_keys_bits_0_16_ms"] = time_events(s32, reps, torch, stream)
+    same = bool(torch.equal(keys_out, torch.sort(d_values, stable=True)[0])) if n <= 1 << 28 else None
+    del temp, keys_out
+    k16 = d_values.to(torch.int16)
+    k16_out = torch.empty_like(k16)
+    tb = int(lib.speedref_sort_pairs_u16_bytes(n))
+    temp = torch.empty(tb, dtype=torch.uint8, device=dev)
+
+    def s16():
+        assert lib.speedref_sort_pairs_u16(k16.data_ptr(), k16_out.data_ptr(), rids.data_ptr(),
+                                           vals_out.data_ptr(), n, temp.data_ptr(), tb, sh) == 0
+    s16()
+    out["u16_keys_ms"] = time_events(s16, reps, torch, stream)
+    out["sorted_keys_check"] = same
+    del temp, k16, k16_out, rids, vals_out
+    torch.cuda.empty_cache()
+    return out
+
+
+def gen_batched(ncols: int, seed: int, torch, dev):
+    """C4 columns: rows log-uniform in [1,024, 4,194,304], cardinality
+    log-uniform in [2, 65,536], values uniform within it (seeded, on the
+    device).  Returns (sizes, cards, device columns)."""
+    rng = np.random.default_rng(seed)
+    sizes = np.rint(np.exp(rng.uniform(np.log(1024), np.log(4194304), ncols))).astype(np.int64)
+    cards = np.rint(np.exp(rng.uniform(np.log(2), np.log(65536), ncols))).astype(np.int64)
+    g = torch.Generator(device=dev)
+    g.manual_seed(seed)
+    cols = [torch.randint(0, int(c), (int(n),), generator=g, device=dev, dtype=torch.int32)
+            for n, c in zip(sizes, cards)]
+    return sizes, cards, cols
+
+
+def bench_batched(args, lib, wah, torch, dev, stream, verify=False):
     """C4: 4,096 columns, rows log-uniform in [1,024, 4,194,304], cardinality
     log-uniform in [2, 65,536], values uniform within it.  Batched (one
     launch sequence, replayed CUDA graph) against the plain path (one
     wah_build per column on the same stream)."""
-    rng = np.random.default_rng(args.seed + 4)
     ncols = args.batch_cols
-    sizes = np.rint(np.exp(rng.uniform(np.log(1024), np.log(4194304), ncols))).astype(np.int64)
-    cards = np.rint(np.exp(rng.uniform(np.log(2), np.log(65536), ncols))).astype(np.int64)
-    g = torch.Generator(device=dev)
-    g.manual_seed(args.seed + 4)
-    cols = [torch.randint(0, int(c), (int(n),), generator=g, device=dev, dtype=torch.int32)
-            for n, c in zip(sizes, cards)]
+    sizes, cards, cols = gen_batched(ncols, args.seed + 4, torch, dev)
     bounds = [int(c) - 1 for c in cards]
     b = wah.Batch(sizes.tolist(), bounds)
     outs = b.set_columns(cols, stream=stream)
@@ -284,13 +467,23 @@ def bench_batched(args, lib, wah, torch, dev, stream):
     counts_p = torch.stack([o[3] for o in outs]).cpu().numpy().view(np.uint32)
     same = bool((counts_p == counts_b).all())
     total = int(sizes.sum())
+    parity = None
+    if verify:
+        # the batched build once more into the outputs (the plain path wrote
+        # them last), then every column against the oracle
+        b.launch_graph(stream)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        bad, count = check_batched_columns(outs, cols, oracle_threads(4194304, 16))
+        parity = {"columns_checked": count, "columns_differ": bad, "ok": not bad and count == ncols,
+                  "seconds": time.perf_counter() - t0}
     b.close()
     del cols, outs, ws
     torch.cuda.empty_cache()
     return {"columns": ncols, "rows": total, "ranges": None,
             "rows_per_s_batched": total / (ms_batched / 1e3), "ms_batched": ms_batched,
             "rows_per_s_plain": total / (ms_plain / 1e3), "ms_plain": ms_plain,
-            "speedup": ms_plain / ms_batched, "same_counts_as_plain": same}
+            "speedup": ms_plain / ms_batched, "same_counts_as_plain": same, "parity": parity}
 
 
 def column_text(col, max_digits, torch):
@@ -495,61 +688,267 @@ def bench_c1(args, lib, wah, torch, dev, stream):
             "keycnt": int(c[0]), "index_len": int(c[1]), "merged": int(c[2])}
 
 
-def bench_serving(args, wah, torch, dev):
-    """C5: Poisson arrivals of index-build requests (one pinned host column
-    each), rows log-uniform in [10,000, 16,777,216], values uniform [0,65535],
-    Zipf s=1.1 over 65,536 or run-clustered (mean run 1,000), 1/3 each;
-    64 GB device budget, results kept on the device.  Offered load: 80% of
-    the batching server's capacity measured on a saturating prefix of the
-    trace.  The continuous-batching server and the plain per-request server
-    replay the same trace."""
-    rng = np.random.default_rng(args.seed + 5)
-    nreq = args.serve_requests
-    max_rows = 16_777_216
-    sizes = np.rint(np.exp(rng.uniform(np.log(10_000), np.log(max_rows), nreq))).astype(np.int64)
+SERVE_MAX_ROWS = 16_777_216
+SERVE_KINDS = ("uniform", "zipf1.1", "runs1000")
+
+
+def gen_serving(nreq: int, seed: int, torch, dev):
+    """C5 trace: per request, rows log-uniform in [10,000, 16,777,216] and
+    one of three value distributions (uniform [0, 65535], Zipf s=1.1 over
+    65,536, run-clustered with mean run 1,000), 1/3 each.  A request's column
+    is the first rows of its distribution's 16,777,216-value pool (seeded).
+    Returns (rng, sizes, kinds, pinned host pools, device pools); rng then
+    draws the arrival gaps."""
+    rng = np.random.default_rng(seed)
+    sizes = np.rint(np.exp(rng.uniform(np.log(10_000), np.log(SERVE_MAX_ROWS),
+                                       nreq))).astype(np.int64)
     kinds = rng.integers(0, 3, nreq)
-    pools = []
-    for kind in ("uniform", "zipf1.1", "runs1000"):
-        v = gen_skewed(kind, max_rows, args.seed + 5, torch, dev) if kind != "uniform" else \
-            torch.randint(0, 65536, (max_rows,), device=dev, dtype=torch.int32)
-        h = torch.empty(max_rows, dtype=torch.int32, pin_memory=True)
+    host, devp = [], []
+    for kind in SERVE_KINDS:
+        if kind == "uniform":
+            g = torch.Generator(device=dev)
+            g.manual_seed(seed)
+            v = torch.randint(0, 65536, (SERVE_MAX_ROWS,), generator=g, device=dev,
+                              dtype=torch.int32)
+        else:
+            v = gen_skewed(kind, SERVE_MAX_ROWS, seed, torch, dev)
+        h = torch.empty(SERVE_MAX_ROWS, dtype=torch.int32, pin_memory=True)
         h.copy_(v)
-        pools.append(h)
-    del v
+        host.append(h)
+        devp.append(v)
+    return rng, sizes, kinds, host, devp
+
+
+def serve_trace(wah, sizes, kinds, pools, arrivals, count, plain, budget_gb, on_result=None):
+    """Replays the first `count` requests of a trace through a server
+    (continuous batching, or plain per-request builds); on_result(i, rid,
+    res, server), if given, sees every completed request before it is
+    released."""
+    srv = wah.Server(budget_bytes=budget_gb << 30, max_batch=512, streams=3, plain=plain)
+    ids = [srv.submit(pools[int(kinds[i])][:int(sizes[i])], bound=65535,
+                      delay=float(arrivals[i])) for i in range(count)]
+    t0 = time.perf_counter()
+    lat = np.empty(count)
+    for i, rid in enumerate(ids):
+        r = srv.wait(rid)
+        lat[i] = r.latency_s
+        if on_result is not None:
+            on_result(i, rid, r, srv)
+        srv.release(rid)
+    wall = time.perf_counter() - t0
+    srv.close()
+    rows = int(sizes[:count].sum())
+    return {"requests": count, "rows": rows, "wall_s": wall, "rows_per_s": rows / wall,
+            "p50_ms": float(np.percentile(lat, 50) * 1e3),
+            "p99_ms": float(np.percentile(lat, 99) * 1e3), "mean_ms": float(lat.mean() * 1e3)}
+
+
+class _DeviceWords:
+    """A device buffer of n 32-bit words seen by torch without a copy."""
+
+    def __init__(self, ptr: int, n: int):
+        self.__cuda_array_interface__ = {"shape": (n,), "typestr": "<i4", "data": (ptr, False),
+                                         "version": 3, "strides": None}
+
+
+def result_hash(torch, keys, offsets, index, K: int, L: int, k: int, mult):
+    """64-bit fingerprint of one index (a 0-d int64 device tensor, nothing
+    synchronised): every word times a fixed random odd multiplier of its
+    position, summed in wrapping int64 arithmetic (exact and order-free), for
+    index, keys and offsets, mixed with K, L and k."""
+    def part(t, n, base):
+        if n == 0:
+            return torch.zeros((), dtype=torch.int64, device=mult.device)
+        return (t[:n].to(torch.int64) * mult[base:base + n]).sum()
+    return (part(index, L, 0) * 3 + part(keys, K, 7) * 5 + part(offsets, K, 13) * 7
+            + (K * 11 + L * 13 + k * 17))
+
+
+def hash_multipliers(torch, dev, n: int, seed: int):
+    g = torch.Generator(device=dev)
+    g.manual_seed(seed)
+    return torch.randint(-2**62, 2**62, (n + 16,), generator=g, device=dev,
+                         dtype=torch.int64) | 1
+
+
+def verify_serving(lib, wah, torch, dev, sizes, kinds, pools, dpools, arrivals, count,
+                   budget_gb, oracle_sample: int, seed: int, threads: int):
+    """Every request of the trace served again by the continuous-batching
+    server and fingerprinted on the device as it completes (result_hash,
+    before its release), then every request built alone with wah_build and
+    fingerprinted the same way: the two must agree for every request.  A
+    seeded sample of served results is also compared word for word with the
+    oracle.  Returns the counts checked and the mismatches."""
+    from concurrent.futures import ThreadPoolExecutor
+    from oracle import oracle as O
+    O._load()
+    kc, ic = wah.output_caps(SERVE_MAX_ROWS, 65535)
+    mult = hash_multipliers(torch, dev, ic, seed)
+    served_h = torch.zeros(count, dtype=torch.int64, device=dev)
+    alone_h = torch.zeros(count, dtype=torch.int64, device=dev)
+    status = np.zeros(count, dtype=np.int64)
+    stream = torch.cuda.current_stream(dev)
+    sh = stream.cuda_stream
+    pick = set(np.random.default_rng(seed).choice(count, size=min(oracle_sample, count),
+                                                  replace=False).tolist())
+    jobs = []
+    ex = ThreadPoolExecutor(max_workers=threads)
+
+    def on_result(i, rid, res, srv):
+        c = res.counts
+        K, L, k = int(c.keycnt), int(c.index_len), int(c.merged)
+        status[i] = c.status
+        keys = torch.as_tensor(_DeviceWords(res.keys, K), device=dev) if K else None
+        offs = torch.as_tensor(_DeviceWords(res.offsets, K), device=dev) if K else None
+        index = torch.as_tensor(_DeviceWords(res.index, L), device=dev) if L else None
+        served_h[i] = result_hash(torch, keys, offs, index, K, L, k, mult)
+        if i in pick:
+            got = (int(c.status), K, L, k,
+                   *(np.empty(0, np.uint32) if t is None else t.cpu().numpy().view(np.uint32)
+                     for t in (keys, offs, index)))
+            n, kind = int(sizes[i]), int(kinds[i])
+            jobs.append((i, ex.submit(same_as_oracle, pools[kind][:n].numpy().view(np.uint32),
+                                      got)))
+        stream.synchronize()  # the arena memory is reused once released
+
+    serve_trace(wah, sizes, kinds, pools, arrivals, count, False, budget_gb, on_result)
+    # every request alone, fingerprinted the same way
+    alone = wah._Buffers(SERVE_MAX_ROWS, 65535, dev)
+    for i in range(count):
+        n, kind = int(sizes[i]), int(kinds[i])
+        rc = lib.wah_build(dpools[kind].data_ptr(), n, 65535, alone.keys.data_ptr(),
+                           alone.offsets.data_ptr(), alone.index.data_ptr(),
+                           alone.counts.data_ptr(), alone.ws.data_ptr(), alone.ws_bytes, sh)
+        assert rc == 0
+        c = alone.counts.cpu().numpy().view(np.uint32)
+        if c[3] != 0:
+            alone_h[i] = -1
+            continue
+        alone_h[i] = result_hash(torch, alone.keys, alone.offsets, alone.index, int(c[0]),
+                                 int(c[1]), int(c[2]), mult)
+    same = (served_h == alone_h).cpu().numpy() & (status == 0)
+    differ = np.flatnonzero(~same).tolist()
+    oracle_bad = [i for i, f in jobs if not f.result()]
+    ex.shutdown()
+    del alone, served_h, alone_h, mult
     torch.cuda.empty_cache()
+    return {"requests": count, "equal_alone": int(same.sum()), "differ_alone": differ[:20],
+            "compare": "64-bit fingerprint of keys, offsets, index, K, L, k per request",
+            "oracle_checked": len(jobs), "oracle_differ": oracle_bad,
+            "ok": not differ and not oracle_bad}
 
-    def run(plain, arrivals, count):
-        srv = wah.Server(budget_bytes=args.serve_budget_gb << 30, max_batch=512, streams=3,
-                         plain=plain)
-        ids = [srv.submit(pools[int(kinds[i])][:int(sizes[i])], bound=65535,
-                          delay=float(arrivals[i])) for i in range(count)]
-        t0 = time.perf_counter()
-        lat = np.empty(count)
-        for i, rid in enumerate(ids):
-            r = srv.wait(rid)
-            lat[i] = r.latency_s
-            srv.release(rid)
-        wall = time.perf_counter() - t0
-        srv.close()
-        rows = int(sizes[:count].sum())
-        return {"requests": count, "rows": rows, "wall_s": wall,
-                "rows_per_s": rows / wall,
-                "p50_ms": float(np.percentile(lat, 50) * 1e3),
-                "p99_ms": float(np.percentile(lat, 99) * 1e3),
-                "mean_ms": float(lat.mean() * 1e3)}
 
+def bench_serving(args, lib, wah, torch, dev, verify: bool):
+    """C5: Poisson arrivals of index-build requests (one pinned host column
+    each, the trace of gen_serving); 64 GB device budget, results kept on the
+    device.  Offered load: 80% of the batching server's capacity measured on
+    a saturating prefix of the trace.  The continuous-batching server and the
+    plain per-request server replay the same trace; then (outside the timed
+    replays) every request is served again and compared with itself built
+    alone, and a sample with the oracle."""
+    nreq = args.serve_requests
+    rng, sizes, kinds, pools, dpools = gen_serving(nreq, args.seed + 5, torch, dev)
+    torch.cuda.empty_cache()
+    budget = args.serve_budget_gb
     # capacity: a saturating prefix, everything arriving at once
     cal = min(nreq, max(200, nreq // 10))
-    cap = run(False, np.zeros(cal), cal)["rows_per_s"]
+    cap = serve_trace(wah, sizes, kinds, pools, np.zeros(cal), cal, False, budget)["rows_per_s"]
     rate = 0.8 * cap / float(sizes.mean())  # requests per second
     arrivals = np.cumsum(rng.exponential(1.0 / rate, nreq))
-    batched = run(False, arrivals, nreq)
-    plain = run(True, arrivals, nreq)
-    return {"requests": nreq, "offered_rows_per_s": 0.8 * cap, "capacity_rows_per_s": cap,
-            "arrival_rate_per_s": rate, "budget_gb": args.serve_budget_gb,
-            "batched": batched, "plain": plain,
-            "rows_per_s_ratio": batched["rows_per_s"] / plain["rows_per_s"],
-            "results_on_device": True}
+    batched = serve_trace(wah, sizes, kinds, pools, arrivals, nreq, False, budget)
+    plain = serve_trace(wah, sizes, kinds, pools, arrivals, nreq, True, budget)
+    out = {"requests": nreq, "offered_rows_per_s": 0.8 * cap, "capacity_rows_per_s": cap,
+           "arrival_rate_per_s": rate, "budget_gb": budget,
+           "batched": batched, "plain": plain,
+           "rows_per_s_ratio": batched["rows_per_s"] / plain["rows_per_s"],
+           "results_on_device": True}
+    if verify:
+        out["parity"] = verify_serving(lib, wah, torch, dev, sizes, kinds, pools, dpools,
+                                       arrivals, nreq, budget, 64, args.seed + 55,
+                                       oracle_threads(SERVE_MAX_ROWS, 16))
+    del pools, dpools
+    torch.cuda.empty_cache()
+    return out
+
+
+# ---------------------------------------------------------------------------
+# Parity checks against the oracle, outside every timed region.  The oracle
+# (the plain-C restatement of the reference `cpu` program) runs on host
+# threads (ctypes releases the GIL); each column's GPU result is compared
+# word for word: keys, offsets, index, and the merged-entry count.
+# ---------------------------------------------------------------------------
+def host_mem_available() -> int:
+    try:
+        with open("/proc/meminfo") as f:
+            for line in f:
+                if line.startswith("MemAvailable:"):
+                    return int(line.split()[1]) * 1024
+    except OSError:
+        pass
+    return 0
+
+
+def oracle_threads(max_rows: int, want: int) -> int:
+    """Concurrent oracle builds of up to max_rows rows that fit in host
+    memory (about 56 bytes per row each, with the GPU result held beside it)."""
+    avail = host_mem_available()
+    fit = int(avail * 0.7 // max(56 * max_rows, 1)) if avail else 1
+    return max(1, min(want, fit, os.cpu_count() or 1))
+
+
+def result_numpy(keys, offsets, index, counts):
+    """(status, K, L, k, keys[K], offsets[K], index[L]) of one device result."""
+    c = counts.cpu().numpy().view(np.uint32)
+    K, L = int(c[0]), int(c[1])
+    return (int(c[3]), K, L, int(c[2]), keys[:K].cpu().numpy().view(np.uint32),
+            offsets[:K].cpu().numpy().view(np.uint32), index[:L].cpu().numpy().view(np.uint32))
+
+
+def same_as_oracle(values: np.ndarray, got) -> bool:
+    """got = result_numpy(...); True when it equals the oracle's index of values."""
+    from oracle import oracle as O
+    status, K, L, k, keys, offs, index = got
+    ref = O.build(values)
+    return (status == 0 and k == ref.merged and np.array_equal(keys, ref.keys)
+            and np.array_equal(offs, ref.offsets) and np.array_equal(index, ref.index))
+
+
+def check_columns(jobs, threads: int):
+    """jobs: iterable of (values numpy, got) pairs, or of callables returning
+    one; oracle builds on `threads` host threads.  Returns the indexes of the
+    columns that differ and the number checked."""
+    from concurrent.futures import ThreadPoolExecutor
+    from oracle import oracle as O
+    O._load()
+
+    def one(job):
+        v, got = job() if callable(job) else job
+        return same_as_oracle(v, got)
+    bad, count = [], 0
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        for i, ok in enumerate(ex.map(one, jobs)):
+            count += 1
+            if not ok:
+                bad.append(i)
+    return bad, count
+
+
+def check_batched_columns(outs, cols, threads: int, group_rows: int = 1 << 28):
+    """Every column of a batch against the oracle: inputs and outputs come to
+    the host a group of columns at a time (bounded host memory)."""
+    bad, count, i = [], 0, 0
+    while i < len(cols):
+        j, rows = i, 0
+        while j < len(cols) and (j == i or rows + cols[j].numel() <= group_rows):
+            rows += cols[j].numel()
+            j += 1
+        jobs = [(cols[c].cpu().numpy().view(np.uint32), result_numpy(*outs[c]))
+                for c in range(i, j)]
+        b, n = check_columns(jobs, threads)
+        bad += [i + x for x in b]
+        count += n
+        i = j
+    return bad, count
 
 
 def cpu_oracle_rate(values: np.ndarray, sample: int, threads: int, repeats: int):
@@ -599,38 +998,64 @@ def cpu_bubble_time(values: np.ndarray, n: int):
     return time.perf_counter() - t0
 
 
+def workload_config(args, n: int, card: int, bound: int, world: int) -> dict:
+    """The `config` of the default workload, the same on both arms."""
+    return {"workload": f"plain method, one column of {n} uint32 i.i.d. uniform "
+                        f"[0,{card - 1}] (seed {args.seed}+rank), bound {bound}",
+            "rows": n, "bound": bound, "parallelism": f"replicas x{world}",
+            "l2": "inputs larger than L2 (1 GiB column), no flush"}
+
+
 def run_reference(args):
+    """The reference's CPU implementation of the path on this host: the
+    oracle port of the reference `cpu` program (its own sources do not
+    travel to the GPU machine), which is sequential, so one thread.  Each step
+    builds the index of a contiguous slice of --ref-sample rows of the same
+    seeded column as the GPU arm (slices taken in turn), so that the whole
+    run stays within a few minutes; rows/s = rows built / time.  A labelled
+    extra figure runs one slice per host thread at once."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     from oracle import oracle as O
     O.make()
-    n = args.n
-    card = args.card
-    values = gen_uniform(min(n, max(args.cpu_sample * 4, 1 << 22)), card, args.seed)
-    threads = os.cpu_count() or 1
-    sample = min(args.cpu_sample, values.size)
-    for _ in range(max(args.warmup, 0)):
-        cpu_oracle_rate(values, sample, threads, 1)
-    times = []
-    for _ in range(args.steps):
-        r, dt = cpu_oracle_rate(values, sample, threads, 1)
-        times.append(dt)
+    O._load()
+    n, card = args.n, args.card
+    bound = card - 1 if args.bound is None else args.bound
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    values = gen_uniform(n, card, args.seed)
+    sample = min(args.ref_sample, n)
+    nslices = max(n // sample, 1)
+
+    def one(step):
+        lo = (step % nslices) * sample
+        t0 = time.perf_counter()
+        O.build(values[lo:lo + sample])
+        return time.perf_counter() - t0
+    for i in range(max(args.warmup, 0)):
+        one(i)
+    times = [one(args.warmup + i) for i in range(args.steps)]
     total = sum(times)
-    rate = threads * sample * args.steps / total
+    rate = sample * args.steps / total
+    threads = os.cpu_count() or 1
+    par_rate, par_dt = cpu_oracle_rate(values, sample, threads, 1)
     line = {
         "impl": "reference", "metric": METRIC, "value": rate, "unit": "rows/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-        "config": {"workload": f"one column, {n} uint32 uniform [0,{card - 1}], seed "
-                               f"{args.seed}", "rows": n, "bound": card - 1},
-        "cpu_baseline": {"value": rate, "unit": "rows/s", "cores": threads, "kind": "port",
-                         "sample": f"{threads} threads x one oracle build each of {sample} "
-                                   f"rows (disjoint slices of the seeded column) per step",
+        "config": workload_config(args, n, card, bound, world),
+        "cpu_baseline": {"value": rate, "unit": "rows/s", "cores": 1, "kind": "port",
+                         "sample": f"per step one oracle build (1 thread, as the reference cpu "
+                                   f"program runs) of a contiguous {sample}-row slice of the "
+                                   f"seeded {n}-row column, slices in turn",
                          "host": host_cpu()},
         "e2e": {"value": rate, "unit": "rows/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
+        "extra_all_threads": {"rows_per_s": par_rate, "threads": threads, "seconds": par_dt,
+                              "note": f"{threads} oracle builds at once, each of its own "
+                                      f"{sample}-row slice of the column (not the reference's "
+                                      f"sequential program: a parallel upper bound for it)"},
     }
     print(json.dumps(line), flush=True)
 
@@ -759,6 +1184,10 @@ def main():
     # dram__bytes_write.sum, one ncu capture of a 67,108,864-row uniform
     # 16-bit column with the same tile shape); traffic grows with rows.
     traffic_per_row = {"histogram": 4.05, "scatter0": 13.03, "scatter1": 11.05, "emit": 11.28}
+    # DRAM bytes per row of each phase (every kernel of it), same capture
+    phase_dram_per_row = {"histogram": 4.05, "pass0": 13.03, "pass1": 13.19, "build": 15.45}
+    dram_bytes = (sum(phase_dram_per_row.values()) * n
+                  if card == 65536 and derive else None)
     per_unit = {"histogram": "4 B/row",
                 "scatter0": ("10 B/row (key in, 16-bit key + rid out)" if mid16
                              else "12 B/row (key in, key + rid out)"),
@@ -811,15 +1240,34 @@ def main():
         pipe.close()
         del pipe, pin_v
 
+    link = None
+    if not args.no_link:
+        link = bench_link(torch, dev, 4 * n, 16 + 8 * K + 4 * L)
+        if e2e is not None:
+            e2e["link"] = {"h2d_gbs": link["h2d_gbs"], "d2h_gbs": link["d2h_gbs"],
+                           "both_gbs": link["both_gbs"], "floor_ms": link["both_ms"],
+                           "ms_over_floor": e2e["ms_per_step"] / link["both_ms"]}
+    cub = None if args.no_cub else bench_cub_sort(torch, dev, d_values, n)
+    if cub is not None:
+        ours = sum(phase_ms[p] for p in ("histogram", "plan", "pass0", "pass1", "pass2", "pass3"))
+        cub["ours_sort_phase_ms"] = ours
+        cub["note"] = ("ours: histogram + digit passes of the index build (16-bit keys between "
+                       "the passes, row ids only out of the last); CUB: SortPairs of the column's "
+                       "(value, row id)")
     decode = None if args.no_decode else bench_decode(args, lib, torch, dev, stream, bufs, n, K, L)
     append = (None if args.no_append else
               bench_append(args, lib, wah, torch, dev, stream, d_values, n, bound, bufs, K, L))
     ingest = None if args.no_ingest else bench_ingest(args, lib, torch, dev, stream, d_values, n)
     c1 = None if args.no_c1 else bench_c1(args, lib, wah, torch, dev, stream)
 
-    skewed = None if args.no_skewed else bench_skewed(args, lib, wah, torch, dev, stream)
-    batched = None if args.no_batched else bench_batched(args, lib, wah, torch, dev, stream)
-    serving = None if args.no_serving else bench_serving(args, wah, torch, dev)
+    verify = not args.no_parity and rank == 0
+    c3_keep = [] if verify else None
+    skewed = (None if args.no_skewed else
+              bench_skewed(args, lib, wah, torch, dev, stream, c3_keep))
+    batched = (None if args.no_batched else
+               bench_batched(args, lib, wah, torch, dev, stream, verify))
+    serving = (None if args.no_serving else
+               bench_serving(args, lib, wah, torch, dev, not args.no_parity))
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -839,6 +1287,31 @@ def main():
                                    "note": "the reference cpu program as written (O(n^2) "
                                            "bubble sort), 1 thread; n^2 extrapolation"}}
 
+    # Oracle checks of the C2 column and the C3 columns (the C4 and C5 checks
+    # ran inside their legs, after their timed parts); nothing here is timed.
+    parity = None
+    if verify:
+        t0 = time.perf_counter()
+        c2_got = result_numpy(bufs.keys, bufs.offsets, bufs.index, bufs.counts)
+        jobs = [(values_np, c2_got)] + [(v, got) for _, v, got in (c3_keep or [])]
+        names = ["c2"] + [f"c3_{kind}" for kind, _, _ in (c3_keep or [])]
+        bad, _ = check_columns(jobs, oracle_threads(n, len(jobs)))
+        parity = {name: i not in bad for i, name in enumerate(names)}
+        if batched is not None and batched.get("parity"):
+            bp = batched["parity"]
+            parity["c4_columns_checked"] = bp["columns_checked"]
+            parity["c4"] = bp["ok"]
+        if serving is not None and serving.get("parity"):
+            sp = serving["parity"]
+            parity["c5_requests_equal_alone"] = sp["equal_alone"]
+            parity["c5_oracle_checked"] = sp["oracle_checked"]
+            parity["c5"] = sp["ok"]
+        parity["ok"] = all(v for k, v in parity.items() if isinstance(v, bool))
+        parity["oracle"] = ("oracle/wah_oracle.c (plain-C restatement of the reference cpu "
+                            "program, pinned to its golden vectors), host threads")
+        parity["seconds"] = time.perf_counter() - t0
+        del jobs, c2_got, c3_keep
+
     if rank == 0:
         cl = clocks.summary()
         line = {
@@ -846,10 +1319,7 @@ def main():
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "u32", "data": "synthetic",
-            "config": {"workload": f"plain method, one column of {n} uint32 i.i.d. uniform "
-                                   f"[0,{card - 1}] (seed {args.seed}+rank), bound {bound}",
-                       "rows": n, "bound": bound, "parallelism": f"replicas x{world}",
-                       "l2": "inputs larger than L2 (1 GiB column), no flush"},
+            "config": workload_config(args, n, card, bound, world),
             "outputs": {"keycnt": K, "index_len": L, "merged": k},
             "sort_items": int(lib.wah_get_tuning()),
             "autotune": tuned,
@@ -864,7 +1334,16 @@ def main():
                 "peak": peak, "unit": "GB/s",
                 "frac": (40 * n + 24 * k + 4 * L + 8 * K) / (ms_per_step / 1e3) / 1e9 / peak,
                 "compulsory_io_bytes": 4 * n + 4 * L + 8 * K,
-                "compulsory_io_gbs": (4 * n + 4 * L + 8 * K) / (ms_per_step / 1e3) / 1e9},
+                "compulsory_io_gbs": (4 * n + 4 * L + 8 * K) / (ms_per_step / 1e3) / 1e9,
+                # what the DRAM actually moves: ncu's dram bytes per row of
+                # every phase (a 67,108,864-row capture of the same column
+                # and kernels) times n, over the same build time
+                "dram_bytes": dram_bytes,
+                "dram_bytes_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per row "
+                                     "and phase at 67,108,864 rows, scaled by rows",
+                "dram_gbs": (dram_bytes / (ms_per_step / 1e3) / 1e9 if dram_bytes else None),
+                "dram_frac": (dram_bytes / (ms_per_step / 1e3) / 1e9 / peak
+                              if dram_bytes else None)},
             "phase_us": {p: round(phase_ms[p] * 1e3, 1) for p in PHASES},
             "roofline": {"bound": "hbm", "kernel": {"scatter0": "k_radix_scatter (pass 0)",
                                                     "scatter1": "k_radix_scatter (pass 1)",
@@ -886,7 +1365,10 @@ def main():
             "append": append,
             "c1": c1,
             "ingest": ingest,
+            "link": link,
+            "cub_sort_reference": cub,
             "cpu_baseline": cpu,
+            "parity": parity,
         }
         print(json.dumps(line), flush=True)
     if dist:

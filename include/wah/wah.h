@@ -201,7 +201,12 @@ void wah_batch_destroy(wah_batch* batch);
  * (src/gpu.cpp:103-261).  plain != 0 builds every request alone with
  * wah_build, one at a time (the per-request baseline).  h_values must stay
  * valid until the request completes.  A request that cannot fit the budget
- * even alone is refused with WAH_ENOMEM.  wah_server_wait blocks until the
+ * even alone is refused with WAH_ENOMEM.  An arrived request that finds no
+ * room waits for batches to finish and for results to be released; with
+ * nothing in flight it fails with WAH_ENOMEM once no released result can
+ * make room (none held, or none released for 2 s while it waits: a client
+ * waiting for it while holding the results that block it).  Releasing each
+ * result once read keeps the arena free.  wah_server_wait blocks until the
  * request is done and fills `result` (device pointers valid until
  * wah_server_release; latency = completion - arrival).
  */

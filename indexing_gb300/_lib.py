@@ -72,6 +72,21 @@ def build(verbose: bool = False, force: bool = False, report=None) -> str:
     return LIB_PATH
 
 
+SPEEDREF_PATH = os.path.join(PKG_DIR, "libwah_speedref.so")
+
+
+def build_speedref(force: bool = False) -> str:
+    """Compile libwah_speedref.so: CUB's radix sort as an external speed
+    reference for the benchmark (not part of the library's ABI)."""
+    src = os.path.join(CSRC, "speedref_cub.cu")
+    if (force or not os.path.exists(SPEEDREF_PATH)
+            or os.path.getmtime(SPEEDREF_PATH) < os.path.getmtime(src)):
+        subprocess.run([nvcc(), "-gencode", "arch=compute_103a,code=sm_103a", "-O3",
+                        "-std=c++17", "-Xcompiler", "-fPIC", "-shared", src, "-o",
+                        SPEEDREF_PATH], check=True)
+    return SPEEDREF_PATH
+
+
 HOST_DIR = os.path.join(PKG_DIR, "host")
 BIN_DIR = os.path.join(PKG_DIR, "bin")
 # host programs: (source, links libwah_gb300.so)

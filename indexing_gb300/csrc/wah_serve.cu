@@ -421,13 +421,31 @@ struct wah_server {
     return true;
   }
 
-  // With nothing in flight, a request that arrived but found no room in the
-  // arena (fragmentation) would wait forever: fail it instead.  Only a pass
-  // that stopped for lack of room counts; one that found nothing arrived yet
-  // (the front request may arrive just after it) does not.
+  // A request that arrived but found no room in the arena, with nothing in
+  // flight: while completed results the client has not released yet hold
+  // arena memory, it waits for their release (a client that reads results
+  // more slowly than they complete); when none are held, or no release has
+  // come for kStallFailS (a client that waits for this request while it
+  // holds the results that block it), it can never be placed: fail it.  Only
+  // a pass that stopped for lack of room counts; one that found nothing
+  // arrived yet (the front request may arrive just after it) does not.
+  static constexpr double kStallFailS = 2.0;
+  double blocked_since = -1.0;  // start of the current stall, -1 when none
+
   void fail_unplaceable() {
     std::lock_guard<std::mutex> lk(mu);
-    if (!mem_blocked || waiting.empty()) return;
+    if (!mem_blocked || waiting.empty()) {
+      blocked_since = -1.0;
+      return;
+    }
+    const size_t ws = plain_ws_off == SIZE_MAX ? 0 : arena_round(plain_ws_bytes);
+    const size_t resident = arena.used() - std::min(arena.used(), ws);
+    const double t = now_s();
+    if (resident > 0) {
+      if (blocked_since < 0) blocked_since = t;
+      if (t - blocked_since < kStallFailS) return;
+    }
+    blocked_since = -1.0;
     mem_blocked = false;
     Req& r = reqs[waiting.front()];
     waiting.pop_front();
@@ -451,7 +469,12 @@ struct wah_server {
         launched = mode == 1 ? launch_plain(b) : launch_batch(b);
         if (launched) break;  // one launch per pass, then reap again
       }
-      if (!launched && !any_busy) fail_unplaceable();
+      if (!launched && !any_busy) {
+        fail_unplaceable();
+      } else {
+        std::lock_guard<std::mutex> lk(mu);
+        blocked_since = -1.0;
+      }
       std::unique_lock<std::mutex> lk(mu);
       if (stop && waiting.empty() &&
           std::none_of(slots.begin(), slots.end(), [](const BatchSlot& b) { return b.busy; }))
@@ -556,6 +579,7 @@ int wah_server_release(wah_server* s, uint64_t id) {
   if (it == s->reqs.end() || it->second.state < 2) return WAH_EINVAL;
   if (it->second.out_bytes) s->arena.release(it->second.out_off, it->second.out_bytes);
   s->reqs.erase(it);
+  s->blocked_since = -1.0;  // progress: a stalled admission waits afresh
   s->cv.notify_all();
   return WAH_OK;
 }
