@@ -99,7 +99,7 @@ int wah_build(const uint32_t* d_values, uint64_t n, uint32_t bound,
  * pool, or a serving loop that cannot afford the device synchronisation of
  * cudaMalloc/cudaFree, passes only the column and the output buffers; the
  * build's scratch memory is a fixed array in the library's device image
- * (22 MiB, held by every GPU that loads the library until exit).  Columns of
+ * (24 MiB, held by every GPU that loads the library until exit).  Columns of
  * up to WAH_NOALLOC_MAX_ROWS rows; larger n returns WAH_ERANGE without
  * enqueueing anything (d_counts is left untouched then, so it does not hold
  * this call's result).  Calls no allocator.  All calls share the array:

@@ -74,8 +74,8 @@ constexpr size_t kAlign = 256;
 inline size_t align_up(size_t x) { return (x + kAlign - 1) / kAlign * kAlign; }
 
 struct WsLayout {
-  size_t ctrl, range_hist, range_start, range_counts, range_first, keyhist, keystart, keys_a,
-      rids_a, keys_b, rids_b, total;
+  size_t ctrl, range_hist, range_start, seg0, range_counts, range_first, keyhist, keystart,
+      keys_a, rids_a, keys_b, rids_b, total;
 };
 
 WsLayout ws_layout(uint64_t n) {
@@ -86,6 +86,8 @@ WsLayout ws_layout(uint64_t n) {
   l.range_hist = off;
   off += align_up((size_t)kDigits * kMaxRanges * kRadix * sizeof(uint32_t));
   l.range_start = off;
+  off += align_up((size_t)kMaxRanges * kRadix * sizeof(uint32_t));
+  l.seg0 = off;
   off += align_up((size_t)kMaxRanges * kRadix * sizeof(uint32_t));
   l.range_counts = off;
   off += align_up((size_t)kMaxRanges * 4 * sizeof(uint32_t));
@@ -126,6 +128,7 @@ void workspace_views(const WsLayout& l, unsigned char* ws, uint64_t n, ColumnVie
   c->derive_ok = 0;
   ra->hist = reinterpret_cast<uint32_t*>(ws + l.range_hist);
   ra->start = reinterpret_cast<uint32_t*>(ws + l.range_start);
+  ra->seg0 = reinterpret_cast<uint32_t*>(ws + l.seg0);
   ra->counts = reinterpret_cast<uint32_t*>(ws + l.range_counts);
   ra->first = reinterpret_cast<uint32_t*>(ws + l.range_first);
   ra->max_ranges = kMaxRanges;

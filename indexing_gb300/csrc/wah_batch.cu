@@ -161,6 +161,7 @@ cudaError_t enqueue_batch(const BatchLayout& L, unsigned char* dev, cudaStream_t
   RangeArrays ra;
   ra.hist = reinterpret_cast<uint32_t*>(dev + L.o_hist);
   ra.start = reinterpret_cast<uint32_t*>(dev + L.o_start);
+  ra.seg0 = nullptr;  // no key-start mode in batches
   ra.counts = reinterpret_cast<uint32_t*>(dev + L.o_counts);
   ra.first = reinterpret_cast<uint32_t*>(dev + L.o_rfirst);
   ra.max_ranges = std::max<uint32_t>(L.nranges, 1);

@@ -22,6 +22,9 @@ constexpr int kRadixBits = 8;
 constexpr int kRadix = 1 << kRadixBits;  // 256 bins per digit
 constexpr int kDigits = 4;               // 32-bit keys -> up to 4 passes
 
+// Packed pass-0 words carry a row's offset in its range in 24 bits.
+constexpr uint64_t kPackRangeRows = 1ull << 24;
+
 // Radix scatter: 256 threads (one per bin), rows per thread a tuning choice
 // (8/12/16).  The column is cut into at most kMaxRanges equal row ranges, one
 // persistent scatter CTA each; histogram/count kernels use
@@ -342,6 +345,12 @@ struct OneColumn {
   ColumnView c;
   uint64_t range_rows;  // multiple of every tile size
   uint32_t ranges;
+  // Key-start mode packs digit pass 0's output (one word per row: the row's
+  // offset in its pass-0 range << 8 | its high digit); the later pass reads
+  // the starts of pass 0's (bin, range) runs, bin-major, to recover row ids.
+  uint32_t ranges0;        // ranges of digit pass 0
+  uint64_t range_rows0;    // rows per pass-0 range (< kPackRangeRows)
+  uint32_t* seg0;          // [256 * ranges0] run starts of pass 0, bin-major
   __device__ __forceinline__ const ColumnView& col(uint32_t) const { return c; }
   __device__ __forceinline__ RangeView range(uint32_t r) const {
     RangeView v;
@@ -371,6 +380,8 @@ struct ManyColumns {
 struct RangeArrays {
   uint32_t* hist;    // [kDigits][max_ranges][256] digit counts per range, zeroed per build
   uint32_t* start;   // [max_ranges][256] first output position per (range, bin)
+  uint32_t* seg0;    // [256][max_ranges] pass-0 run starts, bin-major (key-start mode;
+                     // nullptr where that mode is not used)
   uint32_t* counts;  // [max_ranges][4] words, keys, segments per range
   uint32_t* first;   // [max_ranges][2] first word and key per range
   uint32_t max_ranges;

@@ -567,7 +567,7 @@ cudaError_t launch_build_one(const ColumnView& c, const RangeArrays& ra, const L
   if (err != cudaSuccess) return err;
   uint64_t want = (uint64_t)std::max(o.sm_count, 1) * std::max(per_sm, 1);
   if (want > ra.max_ranges) want = ra.max_ranges;
-  OneColumn g;
+  OneColumn g{};
   g.c = c;
   g.range_rows =
       std::max<uint64_t>(ceil_div(ceil_div(c.n, want), kBuildTile) * kBuildTile, kBuildTile);

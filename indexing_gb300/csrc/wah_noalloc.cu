@@ -31,8 +31,8 @@
 
 namespace {
 
-// Workspace of wah_build for WAH_NOALLOC_MAX_ROWS rows (21.4 MiB), rounded up.
-constexpr size_t kNoAllocBytes = (size_t)22 << 20;
+// Workspace of wah_build for WAH_NOALLOC_MAX_ROWS rows (22.4 MiB), rounded up.
+constexpr size_t kNoAllocBytes = (size_t)24 << 20;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 

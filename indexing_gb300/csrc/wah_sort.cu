@@ -136,15 +136,16 @@ __device__ __forceinline__ void histogram_range16(const uint16_t* __restrict__ k
     for (uint64_t i = lo + chunks * 256 + lane; i < hi; i += 32) wh.add(keys[i], acc_or, acc_nor);
 }
 
-// 16-bit keys in order of their low digit (the pass-0 output): the digit-1
-// counts of the range as histogram_range16 gives them, and every full key
-// counted into keyhist.  A 256-row chunk whose first and last keys share the
-// low digit (all but at most 255 chunks of the column: each low digit's rows
-// are contiguous) counts its keys' high digits into the warp's counters for
-// that low digit, hw, which go to the range's digit-1 counts h1 and to
-// keyhist when the warp's low digit changes (one shared atomic per key, as
-// in histogram_range16); a chunk that spans low digits adds its keys to h1
-// and keyhist one by one.
+// Key-start mode, the count before digit pass 1.  Pass 0 wrote one packed
+// word per row, (row offset in its pass-0 range) << 8 | high digit, in order
+// of the low digit; a row's low digit is the pass-0 bin its position lies in
+// (binoff[d] = first position of bin d, binoff[256] = n).  Counts the high
+// digits of the rows into the range's digit-1 counts h1 and every full key
+// into keyhist.  A 128-row chunk inside one low-digit bin (all but at most
+// 255 chunks of the column) counts its high digits into the warp's counters
+// for that low digit, hw, which go to h1 and keyhist when the warp's low
+// digit changes (one shared atomic per row); a chunk that spans low digits
+// adds its rows to h1 and keyhist one by one.
 __device__ __forceinline__ void flush_keyhist(uint32_t* hw, uint32_t* h1, uint32_t d0,
                                               uint32_t lane, uint32_t* __restrict__ keyhist) {
   __syncwarp();
@@ -159,35 +160,48 @@ __device__ __forceinline__ void flush_keyhist(uint32_t* hw, uint32_t* h1, uint32
   __syncwarp();
 }
 
-__device__ __forceinline__ void histogram_range16_full(const uint16_t* __restrict__ keys,
-                                                       uint64_t lo, uint64_t hi,
-                                                       uint32_t (*s_h)[1][kRadix],
-                                                       uint32_t (*s_full)[kRadix],
-                                                       uint32_t* __restrict__ keyhist) {
+// Low digit of position p: the last bin whose first position is <= p
+// (empty bins share their start with the next bin; the last of them is the
+// bin p is in).
+__device__ __forceinline__ uint32_t bin_of(const uint32_t* binoff, uint32_t p) {
+  uint32_t a = 0;
+#pragma unroll
+  for (uint32_t step = 128; step > 0; step >>= 1)
+    if (binoff[a + step] <= p) a += step;
+  return a;
+}
+
+__device__ __forceinline__ void count_packed_keys(const uint32_t* __restrict__ words, uint64_t lo,
+                                                  uint64_t hi, const uint32_t* binoff,
+                                                  uint32_t (*s_h)[1][kRadix],
+                                                  uint32_t (*s_full)[kRadix],
+                                                  uint32_t* __restrict__ keyhist) {
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const uint32_t nwarps = blockDim.x >> 5;
-  uint32_t* h1 = s_h[warp][0];    // digit-1 counts of the range
-  uint32_t* hw = s_full[warp];    // digit-1 counts for the warp's current low digit
-  uint32_t cur = kRadix;          // the low digit hw counts (none yet)
-  const uint4* kv = reinterpret_cast<const uint4*>(keys + lo);
-  const uint64_t chunks = (hi - lo) / 256;  // 32 lanes x 8 keys
-  auto add_chunk = [&](const uint4& q) {
-    const uint32_t k8[8] = {q.x & 0xFFFFu, q.x >> 16, q.y & 0xFFFFu, q.y >> 16,
-                            q.z & 0xFFFFu, q.z >> 16, q.w & 0xFFFFu, q.w >> 16};
-    const uint32_t first = __shfl_sync(0xffffffffu, k8[0], 0) & 0xFFu;
-    const uint32_t last = __shfl_sync(0xffffffffu, k8[7], 31) & 0xFFu;
-    if (first == last) {
-      if (first != cur) {
+  uint32_t* h1 = s_h[warp][0];  // digit-1 counts of the range
+  uint32_t* hw = s_full[warp];  // digit-1 counts for the warp's current low digit
+  uint32_t cur = kRadix;        // the low digit hw counts (none yet)
+  const uint4* wv = reinterpret_cast<const uint4*>(words + lo);
+  const uint64_t chunks = (hi - lo) / 128;  // 32 lanes x 4 words
+  auto add_chunk = [&](const uint4& q, uint64_t c) {
+    const uint32_t c0 = (uint32_t)(lo + c * 128);
+    const uint32_t d0 = bin_of(binoff, c0);
+    if (c0 + 127 < binoff[d0 + 1]) {
+      if (d0 != cur) {
         if (cur < kRadix) flush_keyhist(hw, h1, cur, lane, keyhist);
-        cur = first;
+        cur = d0;
       }
-#pragma unroll
-      for (int i = 0; i < 8; ++i) atomicAdd(&hw[k8[i] >> 8], 1u);
+      atomicAdd(&hw[q.x & 0xFFu], 1u);
+      atomicAdd(&hw[q.y & 0xFFu], 1u);
+      atomicAdd(&hw[q.z & 0xFFu], 1u);
+      atomicAdd(&hw[q.w & 0xFFu], 1u);
     } else {
+      const uint32_t w4[4] = {q.x, q.y, q.z, q.w};
 #pragma unroll
-      for (int i = 0; i < 8; ++i) {
-        atomicAdd(&h1[k8[i] >> 8], 1u);
-        atomicAdd(&keyhist[k8[i]], 1u);
+      for (int i = 0; i < 4; ++i) {
+        const uint32_t d1 = w4[i] & 0xFFu;
+        atomicAdd(&h1[d1], 1u);
+        atomicAdd(&keyhist[(d1 << 8) | bin_of(binoff, c0 + lane * 4 + i)], 1u);
       }
     }
   };
@@ -195,18 +209,18 @@ __device__ __forceinline__ void histogram_range16_full(const uint16_t* __restric
   for (; c + (kHistUnroll - 1) * nwarps < chunks; c += kHistUnroll * nwarps) {
     uint4 q[kHistUnroll];
 #pragma unroll
-    for (int u = 0; u < kHistUnroll; ++u) q[u] = ld_stream_v4(kv + (c + u * nwarps) * 32 + lane);
+    for (int u = 0; u < kHistUnroll; ++u) q[u] = ld_stream_v4(wv + (c + u * nwarps) * 32 + lane);
 #pragma unroll
-    for (int u = 0; u < kHistUnroll; ++u) add_chunk(q[u]);
+    for (int u = 0; u < kHistUnroll; ++u) add_chunk(q[u], c + u * nwarps);
   }
-  for (; c < chunks; c += nwarps) add_chunk(ld_stream_v4(kv + c * 32 + lane));
+  for (; c < chunks; c += nwarps) add_chunk(ld_stream_v4(wv + c * 32 + lane), c);
   if (cur < kRadix) flush_keyhist(hw, h1, cur, lane, keyhist);
   __syncwarp();
   if (warp == 0)
-    for (uint64_t i = lo + chunks * 256 + lane; i < hi; i += 32) {
-      const uint32_t k = keys[i];
-      atomicAdd(&h1[k >> 8], 1u);
-      atomicAdd(&keyhist[k], 1u);
+    for (uint64_t i = lo + chunks * 128 + lane; i < hi; i += 32) {
+      const uint32_t d1 = words[i] & 0xFFu;
+      atomicAdd(&h1[d1], 1u);
+      atomicAdd(&keyhist[(d1 << 8) | bin_of(binoff, (uint32_t)i)], 1u);
     }
 }
 
@@ -259,17 +273,25 @@ __global__ void __launch_bounds__(kHistThreads)
   const uint32_t* keys = sel_keys(c, src);
   __shared__ uint32_t s_h[kHistWarps][1][kRadix];
   __shared__ uint32_t s_full[kHistWarps][kRadix];
+  __shared__ uint32_t s_binoff[kRadix + 1];
+  const bool packed = c.ctrl->derive && pass == 1;  // key-start mode: packed pass-0 words
   for (int i = threadIdx.x; i < kHistWarps * kRadix; i += kHistThreads) {
     (&s_h[0][0][0])[i] = 0;
     (&s_full[0][0])[i] = 0;
   }
+  if constexpr (std::is_same<G, OneColumn>::value) {
+    // pass-0 bin starts: the run of (bin d, range 0) starts bin d
+    if (packed)
+      for (int d = threadIdx.x; d <= kRadix; d += kHistThreads)
+        s_binoff[d] = d < kRadix ? g.seg0[(uint64_t)d * g.ranges0] : (uint32_t)c.n;
+  }
   __syncthreads();
   uint64_t lo, hi;
   sub_range(rv, blockIdx.x % kCountCtasPerRange, &lo, &hi);
-  if (c.ctrl->derive && pass == 1)  // 16-bit keys in low-digit order
-    histogram_range16_full(reinterpret_cast<const uint16_t*>(keys), lo, hi, s_h, s_full,
-                           c.keyhist);
-  else if (narrow_keys(c, src))
+  if (packed) {
+    if constexpr (std::is_same<G, OneColumn>::value)
+      count_packed_keys(keys, lo, hi, s_binoff, s_h, s_full, c.keyhist);
+  } else if (narrow_keys(c, src))
     histogram_range16<1>(reinterpret_cast<const uint16_t*>(keys), lo, hi, pass, s_h);
   else
     histogram_range<1>(keys, lo, hi, pass, s_h);
@@ -466,6 +488,87 @@ __device__ __forceinline__ uint32_t digit_peers(uint32_t d) {
   }
 }
 
+// PEERS: 0 all items by ballots, 1 all by match.any, 2 the first
+// kHybridMatchItems by match.any and the rest by ballots (the two pipes work
+// in parallel).
+#ifndef WAH_HYBRID_MATCH_NUM
+#define WAH_HYBRID_MATCH_NUM 3  // match.any share of the items: NUM / 8 (measured best)
+#endif
+__host__ __device__ constexpr int kHybridMatchItems(int items) {
+  return items * WAH_HYBRID_MATCH_NUM / 8;
+}
+
+// Stable ranks of a tile's rows within their warp, by digit: dig[j] is item
+// j's digit (item j of lane l in warp w is tile row w*32*ITEMS + j*32 + l);
+// rank[j] receives its rank among the warp's rows of the same digit (not yet
+// offset by the warp's start in the tile).  Peer masks first (independent),
+// then two interleaved counter chains (whA: the first half of the items,
+// whB: the second half; this warp's zeroed 16-bit counters); on return whA
+// holds the warp's count per digit of the first half, whB of the second.
+template <int ITEMS, int PEERS>
+__device__ __forceinline__ void warp_rank(const uint32_t (&dig)[ITEMS], uint32_t (&rank)[ITEMS],
+                                          uint16_t* whA, uint16_t* whB) {
+  constexpr int HALF = ITEMS / 2;
+  const uint32_t lt = lanemask_lt(), gt = lanemask_gt();
+#pragma unroll
+  for (int j = 0; j < ITEMS; ++j) {
+    const bool ballot = PEERS == 0 || (PEERS == 2 && j >= kHybridMatchItems(ITEMS));
+    rank[j] = ballot ? digit_peers<true>(dig[j]) : digit_peers<false>(dig[j]);
+  }
+#pragma unroll
+  for (int j = 0; j < HALF; ++j) {
+    const uint32_t pa = rank[j], pb = rank[j + HALF];
+    const uint32_t da = dig[j], db = dig[j + HALF];
+    const uint32_t ca = whA[da];
+    const uint32_t cb = whB[db];
+    __syncwarp();
+    if ((pa & gt) == 0) whA[da] = (uint16_t)(ca + __popc(pa));
+    if ((pb & gt) == 0) whB[db] = (uint16_t)(cb + __popc(pb));
+    __syncwarp();
+    rank[j] = ca + __popc(pa & lt);
+    rank[j + HALF] = cb + __popc(pb & lt);
+  }
+#pragma unroll
+  for (int j = HALF; j < ITEMS; ++j) rank[j] += whA[dig[j]];
+}
+
+// Thread b (one per bin), after every warp ranked its rows: the tile's count
+// of bin b, its tile-local start (scan over the bins), each warp's start of
+// bin b in the tile (into whist[w][0][b]), bin_base[b] = the range's next
+// free position of bin b minus the tile-local start, and the running offset
+// advanced by the count.  One barrier inside (the scan); the caller
+// synchronises before anyone reads whist or bin_base.
+__device__ __forceinline__ void tile_bin_starts(uint16_t (*whist)[2][kRadix], uint32_t* run_off,
+                                                uint32_t* bin_base, uint32_t* warp_tmp) {
+  const uint32_t b = threadIdx.x;
+  uint32_t cnt[kSortWarps];
+  uint32_t count = 0;
+#pragma unroll
+  for (int w = 0; w < kSortWarps; ++w) {
+    cnt[w] = whist[w][0][b] + whist[w][1][b];
+    count += cnt[w];
+  }
+  uint32_t tile_total;
+  // (warp totals read here, written again after this tile's later barriers)
+  const uint32_t lstart = block_exclusive_scan_1b<kSortThreads>(count, &tile_total, warp_tmp);
+  uint32_t run = lstart;
+#pragma unroll
+  for (int w = 0; w < kSortWarps; ++w) {
+    whist[w][0][b] = (uint16_t)run;
+    run += cnt[w];
+  }
+  bin_base[b] = run_off[b] - lstart;
+  run_off[b] += count;
+}
+
+// Each warp zeroes its own two counter chains.
+__device__ __forceinline__ void zero_warp_counters(uint16_t* whA, uint32_t lane) {
+  uint4* w4 = reinterpret_cast<uint4*>(whA);
+#pragma unroll
+  for (uint32_t k = lane; k < 2 * kRadix * 2 / 16; k += 32) w4[k] = make_uint4(0, 0, 0, 0);
+  __syncwarp();
+}
+
 // Issue the bulk copies of one whole tile (thread 0 only); k16: the keys are
 // 16-bit (tiles start on multiples of 8 rows, so the copy stays 16-byte aligned).
 __device__ __forceinline__ void fetch_tile(uint32_t* dst_k, uint32_t* dst_r, uint64_t* bar,
@@ -481,20 +584,317 @@ __device__ __forceinline__ void fetch_tile(uint32_t* dst_k, uint32_t* dst_r, uin
   if (rin) bulk_copy_g2s(dst_r, rin + base, rbytes, bar);
 }
 
-// PEERS: 0 all items by ballots, 1 all by match.any, 2 the first
-// kHybridMatchItems by match.any and the rest by ballots (the two pipes work
-// in parallel).
-#ifndef WAH_HYBRID_MATCH_NUM
-#define WAH_HYBRID_MATCH_NUM 3  // match.any share of the items: NUM / 8 (measured best)
-#endif
-__host__ __device__ constexpr int kHybridMatchItems(int items) {
-  return items * WAH_HYBRID_MATCH_NUM / 8;
+// ---------------------------------------------------------------------------
+// Key-start mode (one-column index builds whose keys all fit 16 bits and
+// whose two low digits both vary): the two digit passes exchange one packed
+// word per row instead of a 16-bit key stream beside a row-id stream.
+//
+//  pass 0  ranks rows by the low digit and writes, for each row, its offset
+//          in its pass-0 range << 8 | its high digit (the low digit is
+//          implied by the bin the row lands in, the range start by the run)
+//  pass 1  ranks those words by the high digit and writes row ids; a row's
+//          pass-0 run -- the last run of the bin-major table seg0 starting
+//          at or before the row's position -- gives its range, so
+//          row id = range * range_rows0 + offset.  Every warp follows the
+//          runs itself: the run holding the tile's first row (i0) and the
+//          next 32 run starts in registers; a warp slice of a tile (32 x
+//          ITEMS consecutive rows) mostly holds no run start, and all its
+//          rows then share one base.  A slice with 32 or more run starts
+//          after i0 searches seg0 in global memory row by row.
+//
+// Both kernels keep three tile buffers and issue the bulk copy of tile i + 2
+// after the first barrier of tile i (every thread has finished tile i - 1 by
+// then, whose buffer the copy reuses), so there is no barrier at the end of
+// a tile and warps that finish writing start ranking the next tile.
+// ---------------------------------------------------------------------------
+constexpr int kPackBufs = 3;  // input tiles in flight: the copy of tile i + 2 runs during tile i
+
+template <int ITEMS>
+struct PackSmem {
+  uint32_t in[kPackBufs][kSortThreads * ITEMS];  // input tiles; the current one then holds
+                                                  // the staged rows
+  uint8_t bins[kSortThreads * ITEMS];             // pass 1: digit of each staged row
+  uint16_t whist[kSortWarps][2][kRadix];
+  uint32_t run_off[kRadix];
+  uint32_t bin_base[kRadix];
+  uint32_t warp_tmp[kSortWarps + 1];
+  uint64_t bar[kPackBufs];
+  int abort;
+};
+static_assert(sizeof(PackSmem<8>) <= sizeof(ScatterSmem<8>), "packed passes fit the allocation");
+static_assert(sizeof(PackSmem<12>) <= sizeof(ScatterSmem<12>), "packed passes fit the allocation");
+static_assert(sizeof(PackSmem<16>) <= sizeof(ScatterSmem<16>), "packed passes fit the allocation");
+
+// Number of entries of the sorted seg[0, count) that are <= p (warp-wide
+// 32-ary search; every lane returns it).
+__device__ __forceinline__ uint32_t warp_count_le(const uint32_t* __restrict__ seg,
+                                                 uint32_t count, uint32_t p) {
+  const uint32_t lane = threadIdx.x & 31;
+  uint32_t a = 0, b = count;  // the answer lies in [a, b]
+  while (a < b) {
+    const uint32_t step = (b - a + 31) / 32;
+    const uint32_t idx = a + lane * step;
+    const bool le = idx < b && seg[idx] <= p;
+    const uint32_t k = __popc(__ballot_sync(0xffffffffu, le));
+    if (k == 0) {
+      b = a;
+    } else {
+      const uint32_t last = a + (k - 1) * step;
+      const uint32_t nb = a + k * step;
+      a = last + 1;
+      b = nb < b ? nb : b;
+    }
+  }
+  return a;
 }
+
+// Last index of the sorted seg[0, count) whose value is <= p (seg[0] <= p).
+__device__ __forceinline__ uint32_t last_le(const uint32_t* __restrict__ seg, uint32_t count,
+                                            uint32_t p) {
+  uint32_t a = 0, b = count;  // seg[a] <= p; answer in [a, b)
+  while (b - a > 1) {
+    const uint32_t m = a + (b - a) / 2;
+    if (seg[m] <= p) a = m;
+    else b = m;
+  }
+  return a;
+}
+
+template <int ITEMS, int PEERS>
+__device__ __forceinline__ void scatter_pack0(const OneColumn& g,
+                                              const uint32_t* __restrict__ range_start,
+                                              unsigned char* smem_raw) {
+  constexpr uint32_t TILE = kSortThreads * ITEMS;
+  PackSmem<ITEMS>& sm = *reinterpret_cast<PackSmem<ITEMS>*>(smem_raw);
+  const ColumnView& col = g.c;
+  const RangeView rv = g.range(blockIdx.x);
+  const uint32_t* __restrict__ kin = sel_keys(col, col.ctrl->pass_src[0]);
+  uint32_t* __restrict__ out = const_cast<uint32_t*>(sel_keys(col, col.ctrl->pass_dst[0]));
+  uint32_t* status = col.status;
+  const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint64_t lo = rv.lo, hi = rv.hi;
+  {
+    // this range's run start of every bin, also into the bin-major table of
+    // pass-0 runs that the packed later pass reads
+    const uint32_t st = range_start[(uint64_t)blockIdx.x * kRadix + tid];
+    sm.run_off[tid] = st;
+    g.seg0[(uint64_t)tid * g.ranges + blockIdx.x] = st;
+  }
+  if (lo >= hi) return;
+  const uint32_t ntiles = (uint32_t)ceil_div(hi - lo, TILE);
+
+  if (tid == 0) {
+    for (int b = 0; b < kPackBufs; ++b) mbar_init(&sm.bar[b], 1);
+    sm.abort = 0;
+    fence_mbar_init();
+    for (uint32_t t = 0; t < 2; ++t)  // the first two tiles (whole tiles only)
+      if (hi - lo >= (uint64_t)(t + 1) * TILE)
+        fetch_tile(sm.in[t], nullptr, &sm.bar[t], kin, nullptr, lo + (uint64_t)t * TILE, TILE,
+                   false);
+  }
+  __syncthreads();
+
+  const uint32_t row0 = warp * 32 * ITEMS + lane;
+  uint16_t* whA = sm.whist[warp][0];
+  uint16_t* whB = sm.whist[warp][1];
+  uint32_t phase_bits = 0;
+  const uint32_t n32 = (uint32_t)col.n;
+
+  for (uint32_t i = 0, cur = 0; i < ntiles; ++i, cur = cur + 1 == kPackBufs ? 0 : cur + 1) {
+    const uint64_t base = lo + (uint64_t)i * TILE;
+    const uint32_t valid = hi - base < TILE ? (uint32_t)(hi - base) : TILE;
+    zero_warp_counters(whA, lane);
+    uint32_t key[ITEMS];
+    if (valid == TILE) {
+      if (!mbar_wait_bounded(&sm.bar[cur], (phase_bits >> cur) & 1u)) {
+        set_status(status, WAH_ETIMEOUT);
+        sm.abort = 1;
+      }
+      phase_bits ^= 1u << cur;
+      const uint32_t* kp = sm.in[cur] + row0;
+#pragma unroll
+      for (int j = 0; j < ITEMS; ++j) key[j] = kp[j * 32];
+    } else {
+      // ragged last tile: rows past n take digit 255 and rank after every
+      // real row of the tile (never written out)
+#pragma unroll
+      for (int j = 0; j < ITEMS; ++j) {
+        const uint32_t r = row0 + j * 32;
+        key[j] = r < valid ? kin[base + r] : 0xffffffffu;
+      }
+    }
+    uint32_t dig[ITEMS], rank[ITEMS];
+#pragma unroll
+    for (int j = 0; j < ITEMS; ++j) dig[j] = key[j] & 0xFFu;
+    warp_rank<ITEMS, PEERS>(dig, rank, whA, whB);
+    __syncthreads();
+    // every thread is past tile i - 1: its buffer takes tile i + 2
+    if (tid == 0 && i + 2 < ntiles && hi - (base + 2 * TILE) >= TILE) {
+      const uint32_t nb = cur == 0 ? kPackBufs - 1 : cur - 1;
+      fetch_tile(sm.in[nb], nullptr, &sm.bar[nb], kin, nullptr, base + 2 * TILE, TILE, false);
+    }
+    tile_bin_starts(sm.whist, sm.run_off, sm.bin_base, sm.warp_tmp);
+    __syncthreads();
+    // staged word: tile row << 16 | 16-bit key
+    uint32_t* staged = sm.in[cur];
+#pragma unroll
+    for (int j = 0; j < ITEMS; ++j)
+      staged[whA[dig[j]] + rank[j]] = ((row0 + j * 32) << 16) | (key[j] & 0xFFFFu);
+    __syncthreads();
+    if (!sm.abort) {
+      const uint32_t toff = (uint32_t)(base - lo);  // tile's first row in the range
+#pragma unroll 4
+      for (int it = 0; it < ITEMS; ++it) {
+        const uint32_t k = it * kSortThreads + tid;
+        if (k < valid) {
+          const uint32_t w = staged[k];
+          const uint32_t gpos = sm.bin_base[w & 0xFFu] + k;
+          if (gpos < n32) out[gpos] = ((toff + (w >> 16)) << 8) | ((w >> 8) & 0xFFu);
+          else set_status(status, WAH_ECORRUPT);
+        }
+      }
+    }
+  }
+}
+
+template <int ITEMS, int PEERS>
+__device__ __forceinline__ void scatter_pack1(const OneColumn& g,
+                                              const uint32_t* __restrict__ range_start,
+                                              unsigned char* smem_raw) {
+  constexpr uint32_t TILE = kSortThreads * ITEMS;
+  constexpr uint32_t SLICE = 32 * ITEMS;
+  PackSmem<ITEMS>& sm = *reinterpret_cast<PackSmem<ITEMS>*>(smem_raw);
+  const ColumnView& col = g.c;
+  const RangeView rv = g.range(blockIdx.x);
+  const uint32_t* __restrict__ win_in = sel_keys(col, col.ctrl->pass_src[1]);
+  uint32_t* __restrict__ rout = const_cast<uint32_t*>(sel_rids(col, col.ctrl->pass_dst[1]));
+  const uint32_t* __restrict__ seg0 = g.seg0;
+  const uint32_t nseg = g.ranges0 * kRadix;
+  const uint32_t r0 = g.ranges0;
+  const uint32_t rows0 = (uint32_t)g.range_rows0;
+  uint32_t* status = col.status;
+  const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint64_t lo = rv.lo, hi = rv.hi;
+  if (lo >= hi) return;
+  const uint32_t ntiles = (uint32_t)ceil_div(hi - lo, TILE);
+
+  sm.run_off[tid] = range_start[(uint64_t)blockIdx.x * kRadix + tid];
+  if (tid == 0) {
+    for (int b = 0; b < kPackBufs; ++b) mbar_init(&sm.bar[b], 1);
+    sm.abort = 0;
+    fence_mbar_init();
+    for (uint32_t t = 0; t < 2; ++t)  // the first two tiles (whole tiles only)
+      if (hi - lo >= (uint64_t)(t + 1) * TILE)
+        fetch_tile(sm.in[t], nullptr, &sm.bar[t], win_in, nullptr, lo + (uint64_t)t * TILE, TILE,
+                   false);
+  }
+  // every warp: the run holding the range's first row (seg0[0] = 0 <= lo)
+  uint32_t i0 = warp_count_le(seg0, nseg, (uint32_t)lo) - 1;
+  uint32_t ent = i0 + 1 + lane < nseg ? seg0[i0 + 1 + lane] : 0xffffffffu;  // run starts i0+1..
+  __syncthreads();
+
+  const uint32_t row0 = warp * SLICE + lane;
+  uint16_t* whA = sm.whist[warp][0];
+  uint16_t* whB = sm.whist[warp][1];
+  uint32_t phase_bits = 0;
+  const uint32_t n32 = (uint32_t)col.n;
+
+  for (uint32_t i = 0, cur = 0; i < ntiles; ++i, cur = cur + 1 == kPackBufs ? 0 : cur + 1) {
+    const uint64_t base = lo + (uint64_t)i * TILE;
+    const uint32_t valid = hi - base < TILE ? (uint32_t)(hi - base) : TILE;
+    zero_warp_counters(whA, lane);
+    uint32_t word[ITEMS], rid[ITEMS];
+    if (valid == TILE) {
+      if (!mbar_wait_bounded(&sm.bar[cur], (phase_bits >> cur) & 1u)) {
+        set_status(status, WAH_ETIMEOUT);
+        sm.abort = 1;
+      }
+      phase_bits ^= 1u << cur;
+      const uint32_t* wp = sm.in[cur] + row0;
+#pragma unroll
+      for (int j = 0; j < ITEMS; ++j) word[j] = wp[j * 32];
+    } else {
+#pragma unroll
+      for (int j = 0; j < ITEMS; ++j) {
+        const uint32_t r = row0 + j * 32;
+        word[j] = r < valid ? win_in[base + r] : 0xFFu;  // rows past n: digit 255
+      }
+    }
+    // Row ids.  Slot t (1..32) = run i0 + t, its start in lane t-1's ent;
+    // the slice's rows [s0, s1) lie in runs i0 + k0 .. i0 + k1.
+    {
+      const uint32_t s0 = (uint32_t)base + warp * SLICE, s1 = s0 + SLICE;
+      const uint32_t k0 = __popc(__ballot_sync(0xffffffffu, ent <= s0));
+      const uint32_t k1 = __popc(__ballot_sync(0xffffffffu, ent < s1));
+      if (k1 < 32) {
+        const uint32_t mybase = ((i0 + lane) % r0) * rows0;  // first row id of run i0 + lane
+        const uint32_t b0 = __shfl_sync(0xffffffffu, mybase, k0);
+        if (k1 == k0) {
+#pragma unroll
+          for (int j = 0; j < ITEMS; ++j) rid[j] = b0 + (word[j] >> 8);
+        } else {
+#pragma unroll
+          for (int j = 0; j < ITEMS; ++j) {
+            const uint32_t p = s0 + lane + j * 32;
+            uint32_t k = k0;
+            for (uint32_t t = k0; t < k1; ++t) k += __shfl_sync(0xffffffffu, ent, t) <= p;
+            rid[j] = __shfl_sync(0xffffffffu, mybase, k) + (word[j] >> 8);
+          }
+        }
+      } else {
+#pragma unroll
+        for (int j = 0; j < ITEMS; ++j) {
+          const uint32_t p = s0 + lane + j * 32;
+          const uint32_t sidx = last_le(seg0, nseg, p < n32 ? p : n32 - 1);
+          rid[j] = (sidx % r0) * rows0 + (word[j] >> 8);
+        }
+      }
+      // the runs of the next tile
+      if (i + 1 < ntiles) {
+        const uint32_t p_next = (uint32_t)(base + TILE);
+        const uint32_t adv = __popc(__ballot_sync(0xffffffffu, ent <= p_next));
+        i0 = adv < 32 ? i0 + adv : warp_count_le(seg0, nseg, p_next) - 1;
+        ent = i0 + 1 + lane < nseg ? seg0[i0 + 1 + lane] : 0xffffffffu;
+      }
+    }
+    uint32_t dig[ITEMS], rank[ITEMS];
+#pragma unroll
+    for (int j = 0; j < ITEMS; ++j) dig[j] = word[j] & 0xFFu;
+    warp_rank<ITEMS, PEERS>(dig, rank, whA, whB);
+    __syncthreads();
+    // every thread is past tile i - 1: its buffer takes tile i + 2
+    if (tid == 0 && i + 2 < ntiles && hi - (base + 2 * TILE) >= TILE) {
+      const uint32_t nb = cur == 0 ? kPackBufs - 1 : cur - 1;
+      fetch_tile(sm.in[nb], nullptr, &sm.bar[nb], win_in, nullptr, base + 2 * TILE, TILE, false);
+    }
+    tile_bin_starts(sm.whist, sm.run_off, sm.bin_base, sm.warp_tmp);
+    __syncthreads();
+    uint32_t* staged = sm.in[cur];
+#pragma unroll
+    for (int j = 0; j < ITEMS; ++j) {
+      const uint32_t r = whA[dig[j]] + rank[j];
+      staged[r] = rid[j];
+      sm.bins[r] = (uint8_t)dig[j];
+    }
+    __syncthreads();
+    if (!sm.abort) {
+#pragma unroll 4
+      for (int it = 0; it < ITEMS; ++it) {
+        const uint32_t k = it * kSortThreads + tid;
+        if (k < valid) {
+          const uint32_t gpos = sm.bin_base[sm.bins[k]] + k;
+          if (gpos < n32) rout[gpos] = staged[k];
+          else set_status(status, WAH_ECORRUPT);
+        }
+      }
+    }
+  }
+}
+
 template <int ITEMS, int PEERS, class G>
 __global__ void __launch_bounds__(kSortThreads, ITEMS <= 12 ? 3 : 2)
     k_radix_scatter(G g, int pass, const uint32_t* __restrict__ range_start) {
   constexpr uint32_t TILE = kSortThreads * ITEMS;
-  constexpr int HALF = ITEMS / 2;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   ScatterSmem<ITEMS>& sm = *reinterpret_cast<ScatterSmem<ITEMS>*>(smem_raw);
 
@@ -502,6 +902,13 @@ __global__ void __launch_bounds__(kSortThreads, ITEMS <= 12 ? 3 : 2)
   const ColumnView col = g.col(rv.col);
   const int src = col.ctrl->pass_src[pass];
   if (src < 0) return;  // trivial digit: every row in one bin, order unchanged
+  if constexpr (std::is_same<G, OneColumn>::value) {
+    if (col.ctrl->derive) {  // key-start mode: passes 0 and 1 exchange packed words
+      if (pass == 0) scatter_pack0<ITEMS, PEERS>(g, range_start, smem_raw);
+      else scatter_pack1<ITEMS, PEERS>(g, range_start, smem_raw);
+      return;
+    }
+  }
   const int dst = col.ctrl->pass_dst[pass];
   const uint32_t* kin = sel_keys(col, src);
   const uint32_t* rin = sel_rids(col, src);
@@ -532,7 +939,6 @@ __global__ void __launch_bounds__(kSortThreads, ITEMS <= 12 ? 3 : 2)
   __syncthreads();
 
   const uint32_t row0 = warp * 32 * ITEMS + lane;  // tile row of item 0
-  const uint32_t lt = lanemask_lt(), gt = lanemask_gt();
   uint16_t* whA = sm.whist[warp][0];
   uint16_t* whB = sm.whist[warp][1];
   static_assert(kSortThreads * ITEMS < 65536, "tile rows fit the 16-bit counters");
@@ -550,12 +956,7 @@ __global__ void __launch_bounds__(kSortThreads, ITEMS <= 12 ? 3 : 2)
                  base + TILE, TILE, k16_in);
     // Each warp zeroes its own counters (every read of them in the previous
     // tile came before the barrier that closed it).
-    {
-      uint4* w4 = reinterpret_cast<uint4*>(whA);
-#pragma unroll
-      for (uint32_t k = lane; k < 2 * kRadix * 2 / 16; k += 32) w4[k] = make_uint4(0, 0, 0, 0);
-      __syncwarp();
-    }
+    zero_warp_counters(whA, lane);
     uint32_t key[ITEMS];
     if (valid == TILE) {
       // phases of each buffer's barrier complete in turn; the parity of the
@@ -590,54 +991,12 @@ __global__ void __launch_bounds__(kSortThreads, ITEMS <= 12 ? 3 : 2)
       }
     }
 
-    // Peer masks (independent), then two interleaved counter chains.
-    uint32_t rank[ITEMS];
+    uint32_t dig[ITEMS], rank[ITEMS];
 #pragma unroll
-    for (int j = 0; j < ITEMS; ++j) {
-      const bool ballot = PEERS == 0 || (PEERS == 2 && j >= kHybridMatchItems(ITEMS));
-      rank[j] = ballot ? digit_peers<true>(digit8(key[j], pass))
-                       : digit_peers<false>(digit8(key[j], pass));
-    }
-#pragma unroll
-    for (int j = 0; j < HALF; ++j) {
-      const uint32_t pa = rank[j], pb = rank[j + HALF];
-      const uint32_t da = digit8(key[j], pass);
-      const uint32_t db = digit8(key[j + HALF], pass);
-      const uint32_t ca = whA[da];
-      const uint32_t cb = whB[db];
-      __syncwarp();
-      if ((pa & gt) == 0) whA[da] = (uint16_t)(ca + __popc(pa));
-      if ((pb & gt) == 0) whB[db] = (uint16_t)(cb + __popc(pb));
-      __syncwarp();
-      rank[j] = ca + __popc(pa & lt);
-      rank[j + HALF] = cb + __popc(pb & lt);
-    }
-#pragma unroll
-    for (int j = HALF; j < ITEMS; ++j) rank[j] += whA[digit8(key[j], pass)];
+    for (int j = 0; j < ITEMS; ++j) dig[j] = digit8(key[j], pass);
+    warp_rank<ITEMS, PEERS>(dig, rank, whA, whB);
     __syncthreads();
-
-    // Thread b: tile count of bin b, tile-local bin start, warp starts.
-    const uint32_t b = tid;
-    uint32_t cnt[kSortWarps];
-    uint32_t count = 0;
-#pragma unroll
-    for (int w = 0; w < kSortWarps; ++w) {
-      cnt[w] = sm.whist[w][0][b] + sm.whist[w][1][b];
-      count += cnt[w];
-    }
-    uint32_t tile_total;
-    // (warp totals read here, written again after this tile's later barriers)
-    const uint32_t lstart = block_exclusive_scan_1b<kSortThreads>(count, &tile_total, sm.warp_tmp);
-    {
-      uint32_t run = lstart;
-#pragma unroll
-      for (int w = 0; w < kSortWarps; ++w) {
-        sm.whist[w][0][b] = (uint16_t)run;
-        run += cnt[w];
-      }
-    }
-    sm.bin_base[b] = sm.run_off[b] - lstart;
-    sm.run_off[b] += count;
+    tile_bin_starts(sm.whist, sm.run_off, sm.bin_base, sm.warp_tmp);
     __syncthreads();
 
     // Stage in tile-sorted order.
@@ -646,7 +1005,7 @@ __global__ void __launch_bounds__(kSortThreads, ITEMS <= 12 ? 3 : 2)
     const uint32_t rid0 = (uint32_t)base + row0;
 #pragma unroll
     for (int j = 0; j < ITEMS; ++j) {
-      const uint32_t r = whA[digit8(key[j], pass)] + rank[j];
+      const uint32_t r = whA[dig[j]] + rank[j];
       out_keys[r] = key[j];
       sm.out_rids[r] = rin ? rsrc[j * 32] : rid0 + j * 32;
     }
@@ -780,7 +1139,7 @@ static OneColumn one_column_ranges(const ColumnView& c, const SortVariant<OneCol
   if (want > ra.max_ranges) want = ra.max_ranges;
   const uint64_t tile = (uint64_t)kSortThreads * v.items;
   const uint64_t quantum = std::lcm<uint64_t>(tile, kRangeQuantum);
-  OneColumn g;
+  OneColumn g{};
   g.c = c;
   g.range_rows = std::max<uint64_t>(ceil_div(ceil_div(c.n, want), quantum) * quantum, quantum);
   g.ranges = (uint32_t)std::max<uint64_t>(ceil_div(c.n, g.range_rows), 1);
@@ -799,13 +1158,19 @@ cudaError_t launch_sort_one(const ColumnView& c, const RangeArrays& ra, const La
               ? scatter_variant<OneColumn>(o.later_items, o.later_peers, &v1, &per_sm1)
               : scatter_variant<OneColumn>(o.sort_items, o.sort_peers, &v1, &per_sm1);
   if (err != cudaSuccess) return err;
-  if (c.derive_ok && c.passes >= 2) {  // key counts and key starts (derive mode)
+  OneColumn g0 = one_column_ranges(c, v0, per_sm0, ra, o);
+  OneColumn g1 = one_column_ranges(c, v1, per_sm1, ra, o);
+  // Key-start mode packs a row's offset in its pass-0 range into 24 bits and
+  // needs the table of pass-0 runs.
+  if (!ra.seg0 || g0.range_rows >= kPackRangeRows) g0.c.derive_ok = g1.c.derive_ok = 0;
+  g0.ranges0 = g1.ranges0 = g0.ranges;
+  g0.range_rows0 = g1.range_rows0 = g0.range_rows;
+  g0.seg0 = g1.seg0 = ra.seg0;
+  if (g0.c.derive_ok && c.passes >= 2) {  // key counts and key starts (derive mode)
     err = cudaMemsetAsync(c.keyhist, 0, (size_t)65536 * 4, s);
     if (err == cudaSuccess) err = cudaMemsetAsync(c.keystart, 0, ceil_div(c.n, 32) * 4, s);
     if (err != cudaSuccess) return err;
   }
-  const OneColumn g0 = one_column_ranges(c, v0, per_sm0, ra, o);
-  const OneColumn g1 = one_column_ranges(c, v1, per_sm1, ra, o);
   return launch_sort_t<OneColumn>(g0, g0.ranges, v0, g1, g1.ranges, v1, 1, ra, o, s, launches);
 }
 
