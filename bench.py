@@ -237,15 +237,22 @@ def bench_skewed(args, lib, wah, torch, dev, stream, keep=None):
     keep (a list) receives (kind, host values, host result) of each column
     for the oracle check after every timed leg."""
     out = {}
+    tuning = 0
+    if not args.no_autotune and not args.sort_items:
+        # tile shapes timed on a synthetic skewed column of the same size
+        tuning, cached = wah.autotune_workload(wah.WORKLOAD_SKEWED, args.n, 65535, 0,
+                                               args.tune_cache)
+        out["autotune"] = {"workload": "skewed", "tuning": tuning, "from_cache": cached}
     for kind in ("zipf1.1", "distinct16", "runs1000"):
         v = gen_skewed(kind, args.n, args.seed, torch, dev)
         bufs = wah._Buffers(args.n, 65535, dev)
         sh = stream.cuda_stream
 
         def step():
-            rc = lib.wah_build(v.data_ptr(), args.n, 65535, bufs.keys.data_ptr(),
-                               bufs.offsets.data_ptr(), bufs.index.data_ptr(),
-                               bufs.counts.data_ptr(), bufs.ws.data_ptr(), bufs.ws_bytes, sh)
+            rc = lib.wah_build_tuned(v.data_ptr(), args.n, 65535, bufs.keys.data_ptr(),
+                                     bufs.offsets.data_ptr(), bufs.index.data_ptr(),
+                                     bufs.counts.data_ptr(), bufs.ws.data_ptr(), bufs.ws_bytes,
+                                     tuning, sh)
             assert rc == 0
         step()
         ms = time_events(step, max(3, args.steps // 5), torch, stream)
@@ -438,6 +445,18 @@ def gen_batched(ncols: int, seed: int, torch, dev):
     return sizes, cards, cols
 
 
+def batch_tuning(args, wah, total_rows: int, ncols: int):
+    """Tile shapes for batches of many uneven columns: timed on a synthetic
+    mix of 512 columns with the same mean rows per column (the batch runs
+    the shape of digit pass 0 for every pass)."""
+    if args.no_autotune or args.sort_items:
+        return None
+    tcols = min(ncols, 512)
+    t, cached = wah.autotune_workload(wah.WORKLOAD_BATCH, total_rows * tcols // ncols, 65535,
+                                      tcols, args.tune_cache)
+    return {"workload": f"batch of {tcols} columns", "tuning": t, "from_cache": cached}
+
+
 def bench_batched(args, lib, wah, torch, dev, stream, verify=False):
     """C4: 4,096 columns, rows log-uniform in [1,024, 4,194,304], cardinality
     log-uniform in [2, 65,536], values uniform within it.  Batched (one
@@ -446,7 +465,8 @@ def bench_batched(args, lib, wah, torch, dev, stream, verify=False):
     ncols = args.batch_cols
     sizes, cards, cols = gen_batched(ncols, args.seed + 4, torch, dev)
     bounds = [int(c) - 1 for c in cards]
-    b = wah.Batch(sizes.tolist(), bounds)
+    tuned = batch_tuning(args, wah, int(sizes.sum()), ncols)
+    b = wah.Batch(sizes.tolist(), bounds, tuning=tuned["tuning"] if tuned else 0)
     outs = b.set_columns(cols, stream=stream)
     b.launch_graph(stream)
     ms_batched = time_events(lambda: b.launch_graph(stream), 3, torch, stream)
@@ -486,7 +506,8 @@ def bench_batched(args, lib, wah, torch, dev, stream, verify=False):
     return {"columns": ncols, "rows": total, "ranges": None,
             "rows_per_s_batched": total / (ms_batched / 1e3), "ms_batched": ms_batched,
             "rows_per_s_plain": total / (ms_plain / 1e3), "ms_plain": ms_plain,
-            "speedup": ms_plain / ms_batched, "same_counts_as_plain": same, "parity": parity}
+            "speedup": ms_plain / ms_batched, "same_counts_as_plain": same, "parity": parity,
+            "autotune": tuned}
 
 
 def column_text(col, max_digits, torch):
@@ -662,11 +683,15 @@ def bench_c1(args, lib, wah, torch, dev, stream):
     d_v = torch.from_numpy(v.view(np.int32)).to(dev)
     b = wah._Buffers(n, 65535, dev)
     sh = stream.cuda_stream
+    tuning, tuned = 0, None
+    if not args.no_autotune and not args.sort_items:  # shapes of this size, per call
+        tuning, cached = wah.autotune_workload(wah.WORKLOAD_UNIFORM, n, 65535, 0, args.tune_cache)
+        tuned = {"workload": "uniform", "tuning": tuning, "from_cache": cached}
 
     def build():
-        rc = lib.wah_build(d_v.data_ptr(), n, 65535, b.keys.data_ptr(), b.offsets.data_ptr(),
-                           b.index.data_ptr(), b.counts.data_ptr(), b.ws.data_ptr(), b.ws_bytes,
-                           sh)
+        rc = lib.wah_build_tuned(d_v.data_ptr(), n, 65535, b.keys.data_ptr(),
+                                 b.offsets.data_ptr(), b.index.data_ptr(), b.counts.data_ptr(),
+                                 b.ws.data_ptr(), b.ws_bytes, tuning, sh)
         assert rc == 0
     for _ in range(5):
         build()
@@ -674,6 +699,25 @@ def bench_c1(args, lib, wah, torch, dev, stream):
     ms = time_events(build, reps, torch, stream)
     c = b.counts.cpu().numpy().view(np.uint32)
     assert c[3] == 0
+    # the same build captured once into a CUDA graph and replayed (a caller
+    # that rebuilds columns of one size in the same buffers)
+    graph_ms = None
+    try:
+        g = torch.cuda.CUDAGraph()
+        cs = torch.cuda.Stream(dev)
+        with torch.cuda.graph(g, stream=cs, capture_error_mode="thread_local"):
+            rc = lib.wah_build_tuned(d_v.data_ptr(), n, 65535, b.keys.data_ptr(),
+                                     b.offsets.data_ptr(), b.index.data_ptr(),
+                                     b.counts.data_ptr(), b.ws.data_ptr(), b.ws_bytes, tuning,
+                                     cs.cuda_stream)
+        assert rc == 0
+        for _ in range(5):
+            g.replay()
+        graph_ms = time_events(g.replay, reps, torch, torch.cuda.current_stream(dev))
+        cg = b.counts.cpu().numpy().view(np.uint32)
+        assert cg[3] == 0 and int(cg[1]) == int(c[1])
+    except Exception as ex:  # reported, not fatal: the stream figure stands
+        graph_ms = f"graph capture failed: {ex}"
     kc, ic = wah.output_caps(n, 65535)
     pin = {name: torch.empty(size, dtype=torch.int32, pin_memory=True).numpy().view(np.uint32)
            for name, size in (("v", n), ("k", kc), ("o", kc), ("i", ic))}
@@ -686,7 +730,10 @@ def bench_c1(args, lib, wah, torch, dev, stream):
             cnt = ctx.build_into(pin["v"], pin["k"], pin["o"], pin["i"])
         host_ms = (time.perf_counter() - t0) * 1e3 / 50
     assert int(cnt.keycnt) == int(c[0]) and int(cnt.index_len) == int(c[1])
-    return {"rows": n, "device_us": ms * 1e3, "device_rows_per_s": n / (ms / 1e3),
+    return {"rows": n, "autotune": tuned, "device_us": ms * 1e3,
+            "device_rows_per_s": n / (ms / 1e3),
+            "graph_replay_us": graph_ms * 1e3 if isinstance(graph_ms, float) else graph_ms,
+            "launches": int(lib.wah_last_launch_count()),
             "host_api_us": host_ms * 1e3, "host_api_rows_per_s": n / (host_ms / 1e3),
             "keycnt": int(c[0]), "index_len": int(c[1]), "merged": int(c[2])}
 
@@ -722,12 +769,14 @@ def gen_serving(nreq: int, seed: int, torch, dev):
     return rng, sizes, kinds, host, devp
 
 
-def serve_trace(wah, sizes, kinds, pools, arrivals, count, plain, budget_gb, on_result=None):
+def serve_trace(wah, sizes, kinds, pools, arrivals, count, plain, budget_gb, on_result=None,
+                tuning=0):
     """Replays the first `count` requests of a trace through a server
     (continuous batching, or plain per-request builds); on_result(i, rid,
     res, server), if given, sees every completed request before it is
     released."""
-    srv = wah.Server(budget_bytes=budget_gb << 30, max_batch=512, streams=3, plain=plain)
+    srv = wah.Server(budget_bytes=budget_gb << 30, max_batch=512, streams=3, plain=plain,
+                     tuning=tuning)
     ids = [srv.submit(pools[int(kinds[i])][:int(sizes[i])], bound=65535,
                       delay=float(arrivals[i])) for i in range(count)]
     t0 = time.perf_counter()
@@ -775,7 +824,7 @@ def hash_multipliers(torch, dev, n: int, seed: int):
 
 
 def verify_serving(lib, wah, torch, dev, sizes, kinds, pools, dpools, arrivals, count,
-                   budget_gb, oracle_sample: int, seed: int, threads: int):
+                   budget_gb, oracle_sample: int, seed: int, threads: int, tuning: int = 0):
     """Every request of the trace served again by the continuous-batching
     server and fingerprinted on the device as it completes (result_hash,
     before its release), then every request built alone with wah_build and
@@ -817,7 +866,8 @@ def verify_serving(lib, wah, torch, dev, sizes, kinds, pools, dpools, arrivals, 
                                       got)))
         stream.synchronize()  # the arena memory is reused once released
 
-    serve_trace(wah, sizes, kinds, pools, arrivals, count, False, budget_gb, on_result)
+    serve_trace(wah, sizes, kinds, pools, arrivals, count, False, budget_gb, on_result,
+                tuning=tuning)
     # every request alone, fingerprinted the same way
     alone = wah._Buffers(SERVE_MAX_ROWS, 65535, dev)
     for i in range(count):
@@ -860,22 +910,25 @@ def bench_serving(args, lib, wah, torch, dev, verify: bool):
     budget = args.serve_budget_gb
     # capacity: a saturating prefix, everything arriving at once
     cal = min(nreq, max(200, nreq // 10))
-    cap = serve_trace(wah, sizes, kinds, pools, np.zeros(cal), cal, False, budget)["rows_per_s"]
+    tuned = batch_tuning(args, wah, int(sizes.sum()), nreq)
+    t = tuned["tuning"] if tuned else 0
+    cap = serve_trace(wah, sizes, kinds, pools, np.zeros(cal), cal, False, budget,
+                      tuning=t)["rows_per_s"]
     rate = 0.8 * cap / float(sizes.mean())  # requests per second
     arrivals = np.cumsum(rng.exponential(1.0 / rate, nreq))
-    batched = serve_trace(wah, sizes, kinds, pools, arrivals, nreq, False, budget)
+    batched = serve_trace(wah, sizes, kinds, pools, arrivals, nreq, False, budget, tuning=t)
     plain = serve_trace(wah, sizes, kinds, pools, arrivals, nreq, True, budget)
     out = {"requests": nreq, "offered_rows_per_s": 0.8 * cap, "capacity_rows_per_s": cap,
            "arrival_rate_per_s": rate, "budget_gb": budget,
            "batched": batched, "plain": plain,
            "rows_per_s_ratio": batched["rows_per_s"] / plain["rows_per_s"],
-           "results_on_device": True}
+           "results_on_device": True, "autotune": tuned}
     if verify:
         t0 = time.perf_counter()
         count = min(nreq, args.serve_verify)
         out["parity"] = verify_serving(lib, wah, torch, dev, sizes, kinds, pools, dpools,
                                        arrivals, count, budget, 64, args.seed + 55,
-                                       oracle_threads(SERVE_MAX_ROWS, 16))
+                                       oracle_threads(SERVE_MAX_ROWS, 16), tuning=t)
         out["parity"]["seconds"] = time.perf_counter() - t0
     del pools, dpools
     torch.cuda.empty_cache()

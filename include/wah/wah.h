@@ -94,6 +94,19 @@ int wah_build(const uint32_t* d_values, uint64_t n, uint32_t bound,
               void* stream);
 
 /*
+ * wah_build with the tile shapes of this call given (the reference's radix
+ * shape is fixed, src/phases.cpp:445-453): `tuning` is a tuning word as
+ * wah_set_tuning takes -- for instance the one wah_autotune_workload chose
+ * for this kind of column -- or 0 for the process default.  Builds with
+ * different words may run at the same time.  WAH_EINVAL for a word that
+ * wah_set_tuning would refuse.
+ */
+int wah_build_tuned(const uint32_t* d_values, uint64_t n, uint32_t bound,
+                    uint32_t* d_keys, uint32_t* d_offsets, uint32_t* d_index,
+                    wah_counts* d_counts, void* d_workspace,
+                    size_t workspace_bytes, int tuning, void* stream);
+
+/*
  * wah_build for callers that cannot allocate device memory (no counterpart in
  * the reference).  An ingest plugin whose host engine owns the device memory
  * pool, or a serving loop that cannot afford the device synchronisation of
@@ -183,6 +196,9 @@ typedef struct wah_column {
 typedef struct wah_batch wah_batch;
 int wah_batch_create(const uint64_t* ns, const uint32_t* bounds, uint32_t ncols,
                      wah_batch** out);
+/* The same with the batch's own tuning word (0 = the process default). */
+int wah_batch_create_tuned(const uint64_t* ns, const uint32_t* bounds,
+                           uint32_t ncols, int tuning, wah_batch** out);
 int wah_batch_set_columns(wah_batch* batch, const wah_column* cols, void* stream);
 int wah_batch_build(wah_batch* batch, void* stream);
 int wah_batch_launch_graph(wah_batch* batch, void* stream);
@@ -221,6 +237,11 @@ typedef struct wah_server_result {
 } wah_server_result;
 int wah_server_create(uint64_t budget_bytes, uint32_t max_batch, uint32_t streams,
                       int plain, wah_server** out);
+/* The same with the server's own tuning word for all its builds (0 = the
+ * process default). */
+int wah_server_create_tuned(uint64_t budget_bytes, uint32_t max_batch,
+                            uint32_t streams, int plain, int tuning,
+                            wah_server** out);
 int wah_server_submit(wah_server* server, const uint32_t* h_values, uint64_t n,
                       uint32_t bound, double arrival_delay_s, uint64_t* id);
 int wah_server_wait(wah_server* server, uint64_t id, wah_server_result* result);
@@ -411,24 +432,52 @@ uint32_t wah_last_launch_count(void);
  * hard-codes its radix shape (src/phases.cpp:445-453). */
 #define WAH_TUNE_MATCH 0x100
 #define WAH_TUNE_HYBRID 0x200
+/* In the shape of digit pass 0: one-column index builds whose keys all fit
+ * 16 bits exchange one packed word per row between the two digit passes
+ * (row offset in its pass-0 range and high digit) whatever the length of
+ * pass 0's runs; without it they do so only when pass-0 ranges hold at least
+ * 65,536 rows, and a 16-bit key beside a row id otherwise. */
+#define WAH_TUNE_PACK 0x400
 #define WAH_TUNE_LATER(shape) ((shape) << 16)
 int wah_set_tuning(int sort_items);
 int wah_get_tuning(void);
 
 /*
  * Autotuner: times every tile shape for all digit passes, then every other
- * shape for the passes after the first (WAH_TUNE_LATER), by index builds of
- * a synthetic column of n rows with values up to bound (the reference's
- * radix shape is fixed, src/phases.cpp:445-453; its radix test program takes
- * it as flags, src/radix.cpp:161-184), applies the fastest, and appends it to the text
- * file cache_path (NULL: no cache) under the key (device name, floor(log2 n),
- * digit passes, format tag "t2" for entries that carry the later passes'
- * shape).  When the cache already holds the key, its entry is applied
- * without timing and *from_cache is 1.  Allocates and frees its own device
- * memory; synchronises.  *chosen receives the tuning applied.
+ * shape for the passes after the first (WAH_TUNE_LATER), then the packed
+ * exchange (WAH_TUNE_PACK) on and off, by index builds of a synthetic column
+ * of n rows with values uniform up to bound (the reference's radix shape is
+ * fixed, src/phases.cpp:445-453; its radix test program takes it as flags,
+ * src/radix.cpp:161-184), applies the fastest as the process default, and
+ * appends it to the text file cache_path (NULL: no cache) under the key
+ * (device name, workload "uniform", floor(log2 n), digit passes, format tag
+ * "t3").  When the cache already holds the key, its entry is applied without
+ * timing and *from_cache is 1.  Allocates and frees its own device memory;
+ * synchronises.  *chosen receives the tuning applied.  Candidates are timed
+ * with the word passed per build, so concurrent builds keep their own shapes.
  */
 int wah_autotune(uint64_t n, uint32_t bound, const char* cache_path, int* chosen,
                  int* from_cache);
+
+/*
+ * Autotuning for one kind of workload, applied nowhere: *chosen receives the
+ * tuning word to pass to wah_build_tuned, wah_batch_create_tuned or
+ * wah_server_create_tuned.  workload: WAH_WORKLOAD_UNIFORM (one column of n
+ * rows, values uniform in [0, bound]), WAH_WORKLOAD_SKEWED (one column, a
+ * power law over [0, bound]: a few values hold most rows) or
+ * WAH_WORKLOAD_BATCH (a batch of ncols columns of about n rows in all, row
+ * counts log-uniform, each column's values uniform below its own log-uniform
+ * cardinality; the batch uses the shape of digit pass 0 for every pass).
+ * Times every tile shape (one-column workloads: then every other shape for
+ * the later passes, and the packed exchange on and off) and caches the
+ * choice under (device, workload, size bucket, digit passes) in cache_path
+ * like wah_autotune.  Allocates and frees its own device memory; synchronises.
+ */
+#define WAH_WORKLOAD_UNIFORM 0
+#define WAH_WORKLOAD_SKEWED 1
+#define WAH_WORKLOAD_BATCH 2
+int wah_autotune_workload(int workload, uint64_t n, uint32_t bound, uint32_t ncols,
+                          const char* cache_path, int* chosen, int* from_cache);
 
 /*
  * Per-phase device timing, the counterpart of the reference's

@@ -39,14 +39,24 @@ from ._lib import wah_counts
 
 __all__ = ["WahError", "WahIndex", "build_index", "sort_rids_by_value", "build_sorted",
            "HostContext", "Pipeline", "Batch", "Server", "decoded_bitmap", "workspace_bytes", "output_caps",
-           "MAX_ROWS", "last_launch_count", "autotune", "decode", "query", "parse_text", "append", "QUERY_KEYS", "QUERY_OR",
-           "QUERY_AND", "QUERY_ANDNOT"]
+           "MAX_ROWS", "last_launch_count", "autotune", "autotune_workload", "decode", "query",
+           "parse_text", "append", "QUERY_KEYS", "QUERY_OR", "QUERY_AND", "QUERY_ANDNOT",
+           "TUNE_MATCH", "TUNE_HYBRID", "TUNE_PACK", "WORKLOAD_UNIFORM", "WORKLOAD_SKEWED",
+           "WORKLOAD_BATCH"]
 
 MAX_ROWS = 1 << 30
 
 WAH_OK, WAH_EINVAL, WAH_ENOMEM, WAH_ECUDA, WAH_ETIMEOUT, WAH_ERANGE, WAH_EOVERFLOW, \
     WAH_ENODEV, WAH_ECORRUPT = range(9)
 QUERY_KEYS, QUERY_OR, QUERY_AND, QUERY_ANDNOT = range(4)
+# tuning word flags (include/wah/wah.h) and autotuner workloads
+TUNE_MATCH, TUNE_HYBRID, TUNE_PACK = 0x100, 0x200, 0x400
+WORKLOAD_UNIFORM, WORKLOAD_SKEWED, WORKLOAD_BATCH = range(3)
+
+
+def tune_later(shape: int) -> int:
+    """The tile shape of the digit passes after the first, in a tuning word."""
+    return shape << 16
 
 
 class WahError(RuntimeError):
@@ -123,6 +133,21 @@ def autotune(n: int, bound: int = 0, cache_path: str | None = None):
     return chosen.value, bool(cached.value)
 
 
+def autotune_workload(workload: int, n: int, bound: int = 0, ncols: int = 0,
+                      cache_path: str | None = None):
+    """Times the tile shapes on synthetic data of one workload (one uniform
+    column, one skewed column, or a batch of ``ncols`` columns of about ``n``
+    rows in all) and returns ``(tuning, from_cache)`` without applying it:
+    pass the word to :func:`build_index`, :class:`Batch` or :class:`Server`."""
+    lib = _lib.load()
+    chosen, cached = ctypes.c_int(), ctypes.c_int()
+    rc = lib.wah_autotune_workload(workload, n, bound, ncols,
+                                   cache_path.encode() if cache_path else None,
+                                   ctypes.byref(chosen), ctypes.byref(cached))
+    _check(rc, "wah_autotune_workload")
+    return chosen.value, bool(cached.value)
+
+
 def _stream_handle(stream) -> int:
     torch = _torch()
     s = stream if stream is not None else torch.cuda.current_stream()
@@ -161,7 +186,7 @@ class _Buffers:
 
 
 def build_index(values, bound: int = 0, stream=None, device="cuda", sync: bool = True,
-                buffers: _Buffers | None = None) -> WahIndex:
+                buffers: _Buffers | None = None, tuning: int = 0) -> WahIndex:
     """Builds the WAH index of one uint32 column on the GPU.
 
     ``values``: numpy uint32 array or 32-bit integer tensor.  ``bound``: the
@@ -169,6 +194,8 @@ def build_index(values, bound: int = 0, stream=None, device="cuda", sync: bool =
     :class:`WahIndex` of CUDA int32 tensors holding uint32 bits (use
     ``.numpy()`` for numpy uint32).  With ``sync=False`` the counters are not
     read back and the full-capacity buffers are returned in a tuple instead.
+    ``tuning``: this build's tile shapes (a tuning word), 0 = the process
+    default.
     """
     lib = _lib.load()
     torch = _torch()
@@ -177,9 +204,9 @@ def build_index(values, bound: int = 0, stream=None, device="cuda", sync: bool =
     if n >= MAX_ROWS:
         raise WahError(WAH_ERANGE, "build_index")
     b = buffers or _Buffers(n, bound, v.device)
-    rc = lib.wah_build(v.data_ptr(), n, bound, b.keys.data_ptr(), b.offsets.data_ptr(),
-                       b.index.data_ptr(), b.counts.data_ptr(), b.ws.data_ptr(), b.ws_bytes,
-                       _stream_handle(stream))
+    rc = lib.wah_build_tuned(v.data_ptr(), n, bound, b.keys.data_ptr(), b.offsets.data_ptr(),
+                             b.index.data_ptr(), b.counts.data_ptr(), b.ws.data_ptr(),
+                             b.ws_bytes, tuning, _stream_handle(stream))
     _check(rc, "wah_build")
     if not sync:
         return b
@@ -460,7 +487,7 @@ class Batch:
     build; ``results()`` returns one :class:`WahIndex` per column.
     """
 
-    def __init__(self, sizes, bounds=None):
+    def __init__(self, sizes, bounds=None, tuning: int = 0):
         self._lib = _lib.load()
         self.sizes = [int(x) for x in sizes]
         self.bounds = [int(x) for x in (bounds if bounds is not None else [0] * len(self.sizes))]
@@ -468,7 +495,8 @@ class Batch:
         ns = (ctypes.c_uint64 * nc)(*self.sizes)
         bs = (ctypes.c_uint32 * nc)(*self.bounds)
         h = ctypes.c_void_p()
-        _check(self._lib.wah_batch_create(ns, bs, nc, ctypes.byref(h)), "wah_batch_create")
+        _check(self._lib.wah_batch_create_tuned(ns, bs, nc, tuning, ctypes.byref(h)),
+               "wah_batch_create")
         self._h = h
         self._cols = None
         self._keep = None
@@ -557,11 +585,11 @@ class Server:
     """
 
     def __init__(self, budget_bytes: int = 64 << 30, max_batch: int = 1024, streams: int = 3,
-                 plain: bool = False):
+                 plain: bool = False, tuning: int = 0):
         self._lib = _lib.load()
         h = ctypes.c_void_p()
-        _check(self._lib.wah_server_create(budget_bytes, max_batch, streams, int(plain),
-                                           ctypes.byref(h)), "wah_server_create")
+        _check(self._lib.wah_server_create_tuned(budget_bytes, max_batch, streams, int(plain),
+                                                 tuning, ctypes.byref(h)), "wah_server_create")
         self._h = h
         self._keep = {}
 

@@ -228,6 +228,15 @@ SIGNATURES = {
     "wah_get_tuning": ([], ctypes.c_int),
     "wah_autotune": ([_u64, _u32, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int),
                       ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
+    "wah_autotune_workload": ([ctypes.c_int, _u64, _u32, _u32, ctypes.c_char_p,
+                               ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)],
+                              ctypes.c_int),
+    "wah_build_tuned": ([_vp, _u64, _u32, _vp, _vp, _vp, _vp, _vp, ctypes.c_size_t, ctypes.c_int,
+                         _vp], ctypes.c_int),
+    "wah_batch_create_tuned": ([ctypes.POINTER(_u64), ctypes.POINTER(_u32), _u32, ctypes.c_int,
+                                ctypes.POINTER(_vp)], ctypes.c_int),
+    "wah_server_create_tuned": ([_u64, _u32, _u32, ctypes.c_int, ctypes.c_int,
+                                 ctypes.POINTER(_vp)], ctypes.c_int),
     "wah_events_create": ([_u32, ctypes.POINTER(_vp)], ctypes.c_int),
     "wah_events_destroy": ([_u32, ctypes.POINTER(_vp)], None),
     "wah_events_elapsed": ([_vp, _vp, ctypes.POINTER(ctypes.c_float)], ctypes.c_int),

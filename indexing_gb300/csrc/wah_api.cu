@@ -53,15 +53,32 @@ int cuda_status(cudaError_t e) {
   return WAH_ECUDA;
 }
 
-LaunchOpts launch_opts(int max_passes, cudaEvent_t* events) {
+// One tile shape: rows per thread | peer mode flag (| WAH_TUNE_PACK in the
+// shape of digit pass 0).
+static bool valid_shape(int t, bool first) {
+  const int items = t & 0xff;
+  if (items != 8 && items != 12 && items != 16) return false;
+  if ((t & WAH_TUNE_MATCH) && (t & WAH_TUNE_HYBRID)) return false;
+  const int flags = WAH_TUNE_MATCH | WAH_TUNE_HYBRID | (first ? WAH_TUNE_PACK : 0);
+  return (t & ~(0xff | flags)) == 0;
+}
+
+bool valid_tuning(int t) {
+  if (t <= 0) return false;
+  const int later = (t >> 16) & 0xffff;
+  return valid_shape(t & 0xffff, true) && (later == 0 || valid_shape(later, false));
+}
+
+LaunchOpts launch_opts(int max_passes, cudaEvent_t* events, int tuning) {
   LaunchOpts o;
-  const int t = g_tuning.load(std::memory_order_relaxed);
+  const int t = tuning ? tuning : g_tuning.load(std::memory_order_relaxed);
   const int first = t & 0xffff;
   const int later = (t >> 16) & 0xffff ? (t >> 16) & 0xffff : first;
   o.sort_items = first & 0xff;
   o.sort_peers = (first & WAH_TUNE_MATCH) ? 1 : (first & WAH_TUNE_HYBRID) ? 2 : 0;
   o.later_items = later & 0xff;
   o.later_peers = (later & WAH_TUNE_MATCH) ? 1 : (later & WAH_TUNE_HYBRID) ? 2 : 0;
+  o.pack_force = (first & WAH_TUNE_PACK) != 0;
   o.max_passes = max_passes;
   o.sm_count = sm_count_current();
   o.events = events;
@@ -83,8 +100,8 @@ WsLayout ws_layout(uint64_t n) {
   size_t off = 0;
   l.ctrl = off;
   off += align_up(sizeof(WahCtrl));
-  l.range_hist = off;
-  off += align_up((size_t)kDigits * kMaxRanges * kRadix * sizeof(uint32_t));
+  l.range_hist = off;  // per-range histograms, then the bin totals of each pass
+  off += align_up((size_t)kDigits * (kMaxRanges + kBinTotCopies) * kRadix * sizeof(uint32_t));
   l.range_start = off;
   off += align_up((size_t)kMaxRanges * kRadix * sizeof(uint32_t));
   l.seg0 = off;
@@ -127,6 +144,7 @@ void workspace_views(const WsLayout& l, unsigned char* ws, uint64_t n, ColumnVie
   c->keystart = reinterpret_cast<uint32_t*>(ws + l.keystart);
   c->derive_ok = 0;
   ra->hist = reinterpret_cast<uint32_t*>(ws + l.range_hist);
+  ra->bintot = ra->hist + (size_t)kDigits * kMaxRanges * kRadix;
   ra->start = reinterpret_cast<uint32_t*>(ws + l.range_start);
   ra->seg0 = reinterpret_cast<uint32_t*>(ws + l.seg0);
   ra->counts = reinterpret_cast<uint32_t*>(ws + l.range_counts);
@@ -167,19 +185,8 @@ size_t wah_workspace_bytes(uint64_t n, uint32_t /*bound*/) { return ws_layout(n)
 
 uint32_t wah_last_launch_count(void) { return g_last_launches; }
 
-// One tile shape: rows per thread | peer mode flag.
-static bool valid_shape(int t) {
-  const int items = t & 0xff;
-  if (items != 8 && items != 12 && items != 16) return false;
-  if ((t & WAH_TUNE_MATCH) && (t & WAH_TUNE_HYBRID)) return false;
-  return (t & ~(0xff | WAH_TUNE_MATCH | WAH_TUNE_HYBRID)) == 0;
-}
-
 int wah_set_tuning(int sort_items) {
-  if (sort_items < 0) return WAH_EINVAL;
-  const int later = (sort_items >> 16) & 0xffff;
-  if (!valid_shape(sort_items & 0xffff) || (later != 0 && !valid_shape(later)))
-    return WAH_EINVAL;
+  if (!valid_tuning(sort_items)) return WAH_EINVAL;
   g_tuning.store(sort_items, std::memory_order_relaxed);
   return WAH_OK;
 }
@@ -189,8 +196,9 @@ int wah_get_tuning(void) { return g_tuning.load(std::memory_order_relaxed); }
 static int build_impl(const uint32_t* d_values, uint64_t n, uint32_t bound, uint32_t* d_keys,
                       uint32_t* d_offsets, uint32_t* d_index, wah_counts* d_counts,
                       void* d_workspace, size_t workspace_bytes, void* stream,
-                      cudaEvent_t* events) {
+                      cudaEvent_t* events, int tuning = 0) {
   g_last_launches = 0;
+  if (tuning != 0 && !valid_tuning(tuning)) return WAH_EINVAL;
   if (!d_counts || !aligned16(d_counts)) return WAH_EINVAL;
   if (n >= WAH_MAX_ROWS) return WAH_ERANGE;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
@@ -213,7 +221,7 @@ static int build_impl(const uint32_t* d_values, uint64_t n, uint32_t bound, uint
   c.status = &d_counts->status;
   c.passes = passes_for_bound(bound);
   c.derive_ok = 1;  // an index build: the sorted keys themselves are never read back
-  const LaunchOpts o = launch_opts(c.passes, events);
+  const LaunchOpts o = launch_opts(c.passes, events, tuning);
   if (o.sm_count <= 0) return WAH_ENODEV;
   e = cudaMemsetAsync(c.ctrl, 0, sizeof(WahCtrl), s);
   if (e != cudaSuccess) return cuda_status(e);
@@ -227,6 +235,13 @@ int wah_build(const uint32_t* d_values, uint64_t n, uint32_t bound, uint32_t* d_
               size_t workspace_bytes, void* stream) {
   return build_impl(d_values, n, bound, d_keys, d_offsets, d_index, d_counts, d_workspace,
                     workspace_bytes, stream, nullptr);
+}
+
+int wah_build_tuned(const uint32_t* d_values, uint64_t n, uint32_t bound, uint32_t* d_keys,
+                    uint32_t* d_offsets, uint32_t* d_index, wah_counts* d_counts,
+                    void* d_workspace, size_t workspace_bytes, int tuning, void* stream) {
+  return build_impl(d_values, n, bound, d_keys, d_offsets, d_index, d_counts, d_workspace,
+                    workspace_bytes, stream, nullptr, tuning);
 }
 
 int wah_events_create(uint32_t count, void** events) {

@@ -144,8 +144,8 @@ void fill_batch_columns(const BatchLayout& L, unsigned char* dev, const wah_colu
 }
 
 cudaError_t enqueue_batch(const BatchLayout& L, unsigned char* dev, cudaStream_t s,
-                          uint32_t* launches) {
-  const LaunchOpts o = launch_opts(L.max_passes, nullptr);
+                          uint32_t* launches, int tuning) {
+  const LaunchOpts o = launch_opts(L.max_passes, nullptr, tuning);
   if (o.sm_count <= 0) return cudaErrorNoDevice;
   ColumnView* d_cols = reinterpret_cast<ColumnView*>(dev + L.o_cols);
   cudaError_t e = cudaMemsetAsync(dev + L.o_ctrl, 0, sizeof(WahCtrl) * L.ncols, s);
@@ -162,6 +162,7 @@ cudaError_t enqueue_batch(const BatchLayout& L, unsigned char* dev, cudaStream_t
   ra.hist = reinterpret_cast<uint32_t*>(dev + L.o_hist);
   ra.start = reinterpret_cast<uint32_t*>(dev + L.o_start);
   ra.seg0 = nullptr;  // no key-start mode in batches
+  ra.bintot = nullptr;
   ra.counts = reinterpret_cast<uint32_t*>(dev + L.o_counts);
   ra.first = reinterpret_cast<uint32_t*>(dev + L.o_rfirst);
   ra.max_ranges = std::max<uint32_t>(L.nranges, 1);
@@ -180,6 +181,7 @@ struct wah_batch {
   ColumnView* h_cols = nullptr;  // pinned staging of the column table
   bool columns_set = false;
   cudaGraphExec_t graph = nullptr;
+  int tuning = 0;  // 0: the process default
 };
 
 extern "C" {
@@ -198,12 +200,19 @@ uint32_t wah_batch_ranges(const wah_batch* b) { return b ? b->L.nranges : 0; }
 
 int wah_batch_create(const uint64_t* ns, const uint32_t* bounds, uint32_t ncols,
                      wah_batch** out) {
+  return wah_batch_create_tuned(ns, bounds, ncols, 0, out);
+}
+
+int wah_batch_create_tuned(const uint64_t* ns, const uint32_t* bounds, uint32_t ncols,
+                           int tuning, wah_batch** out) {
   if (!out || !ns || ncols == 0) return WAH_EINVAL;
   *out = nullptr;
+  if (tuning != 0 && !valid_tuning(tuning)) return WAH_EINVAL;
   for (uint32_t c = 0; c < ncols; ++c)
     if (ns[c] >= WAH_MAX_ROWS) return WAH_ERANGE;
   wah_batch* b = new (std::nothrow) wah_batch;
   if (!b) return WAH_ENOMEM;
+  b->tuning = tuning;
   b->n.assign(ns, ns + ncols);
   b->bound.assign(ncols, 0);
   if (bounds) b->bound.assign(bounds, bounds + ncols);
@@ -249,7 +258,8 @@ int wah_batch_build(wah_batch* b, void* stream) {
   if (!b || !b->columns_set) return WAH_EINVAL;
   uint32_t* launches = last_launches_slot();
   *launches = 0;
-  return cuda_status(enqueue_batch(b->L, b->dev, static_cast<cudaStream_t>(stream), launches));
+  return cuda_status(
+      enqueue_batch(b->L, b->dev, static_cast<cudaStream_t>(stream), launches, b->tuning));
 }
 
 int wah_batch_launch_graph(wah_batch* b, void* stream) {

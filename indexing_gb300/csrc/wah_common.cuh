@@ -22,8 +22,11 @@ constexpr int kRadixBits = 8;
 constexpr int kRadix = 1 << kRadixBits;  // 256 bins per digit
 constexpr int kDigits = 4;               // 32-bit keys -> up to 4 passes
 
-// Packed pass-0 words carry a row's offset in its range in 24 bits.
+// Packed pass-0 words carry a row's offset in its range in 24 bits; they are
+// used where pass-0 ranges hold at least kPackMinRangeRows rows (runs of
+// about 256 rows per bin and range, or more), or when a tuning word asks.
 constexpr uint64_t kPackRangeRows = 1ull << 24;
+constexpr uint64_t kPackMinRangeRows = 1ull << 16;
 
 // Radix scatter: 256 threads (one per bin), rows per thread a tuning choice
 // (8/12/16).  The column is cut into at most kMaxRanges equal row ranges, one
@@ -32,6 +35,10 @@ constexpr uint64_t kPackRangeRows = 1ull << 24;
 constexpr int kSortThreads = 256;
 constexpr int kMaxRanges = 1024;
 constexpr int kCountCtasPerRange = 2;
+// Bin totals of a one-column build are summed in this many copies (each
+// counting CTA adds to copy blockIdx % kBinTotCopies), which spreads the
+// atomics of hundreds of CTAs over as many words per bin.
+constexpr int kBinTotCopies = 16;
 
 
 // Fused index build: 128 threads x 16 rows, blocked.
@@ -351,6 +358,9 @@ struct OneColumn {
   uint32_t ranges0;        // ranges of digit pass 0
   uint64_t range_rows0;    // rows per pass-0 range (< kPackRangeRows)
   uint32_t* seg0;          // [256 * ranges0] run starts of pass 0, bin-major
+  uint32_t* bintot;        // [kBinTotCopies][kDigits][256] rows per bin of each pass
+  uint32_t packed;         // key-start mode exchanges packed words (host-decided)
+  uint32_t count_parts;    // counting CTAs per range (0: kCountCtasPerRange)
   __device__ __forceinline__ const ColumnView& col(uint32_t) const { return c; }
   __device__ __forceinline__ RangeView range(uint32_t r) const {
     RangeView v;
@@ -382,6 +392,8 @@ struct RangeArrays {
   uint32_t* start;   // [max_ranges][256] first output position per (range, bin)
   uint32_t* seg0;    // [256][max_ranges] pass-0 run starts, bin-major (key-start mode;
                      // nullptr where that mode is not used)
+  uint32_t* bintot;  // [kBinTotCopies][kDigits][256] rows per bin, right after hist
+                     // (zeroed with it; one-column builds only, else nullptr)
   uint32_t* counts;  // [max_ranges][4] words, keys, segments per range
   uint32_t* first;   // [max_ranges][2] first word and key per range
   uint32_t max_ranges;
@@ -395,6 +407,7 @@ struct LaunchOpts {
   int later_peers;
   int max_passes;       // digit passes launched (max over the columns)
   int sm_count;
+  int pack_force;       // key-start mode exchanges packed words whatever the run length
   cudaEvent_t* events;  // optional: [2*phase] before, [2*phase+1] after
 };
 
@@ -437,13 +450,15 @@ void fill_batch_columns(const BatchLayout& L, unsigned char* dev, const wah_colu
 // Enqueue the whole build; the column, range and span tables must be in
 // `dev` already (stream-ordered before this).
 cudaError_t enqueue_batch(const BatchLayout& L, unsigned char* dev, cudaStream_t s,
-                          uint32_t* launches);
+                          uint32_t* launches, int tuning = 0);
 
 // Shared host helpers (wah_api.cu).
 int passes_for_bound(uint32_t bound);
 int sm_count_current();
 int cuda_status(cudaError_t e);
-LaunchOpts launch_opts(int max_passes, cudaEvent_t* events);
+// tuning: a tuning word as wah_set_tuning takes, 0 = the process default
+LaunchOpts launch_opts(int max_passes, cudaEvent_t* events, int tuning = 0);
+bool valid_tuning(int tuning);
 uint32_t* last_launches_slot();
 
 }  // namespace wah

@@ -145,6 +145,7 @@ bool grow_pinned(T** p, size_t* cap, size_t want) {
 struct wah_server {
   int device = 0;
   int mode = 0;  // 0 continuous batching, 1 plain
+  int tuning = 0;  // tile shapes of its builds, 0: the process default
   uint32_t max_batch = 1;
   unsigned char* dev = nullptr;
   size_t budget = 0;
@@ -313,7 +314,7 @@ struct wah_server {
       e = cudaMemcpyAsync(ws + L.o_spans, b.h_tables + sizeof(RangeView) * L.nranges,
                           L.spans.size() * 4, cudaMemcpyHostToDevice, b.stream);
     uint32_t launches = 0;
-    if (e == cudaSuccess) e = enqueue_batch(L, ws, b.stream, &launches);
+    if (e == cudaSuccess) e = enqueue_batch(L, ws, b.stream, &launches, tuning);
     wah_counts* gather = reinterpret_cast<wah_counts*>(ws + L.bytes);
     if (e == cudaSuccess) {
       k_gather_counts<<<(unsigned)ceil_div(nc, 256), 256, 0, b.stream>>>(
@@ -399,8 +400,8 @@ struct wah_server {
     if (r.n) e = cudaMemcpyAsync(vals, r.h_values, r.n * 4, cudaMemcpyHostToDevice, b.stream);
     int rc = cuda_status(e);
     if (rc == WAH_OK)
-      rc = wah_build(vals, r.n, r.bound, keys, offs, index, cnt, dev + plain_ws_off,
-                     plain_ws_bytes, b.stream);
+      rc = wah_build_tuned(vals, r.n, r.bound, keys, offs, index, cnt, dev + plain_ws_off,
+                           plain_ws_bytes, tuning, b.stream);
     if (rc == WAH_OK)
       rc = cuda_status(cudaMemcpyAsync(b.h_counts, cnt, sizeof(wah_counts),
                                        cudaMemcpyDeviceToHost, b.stream));
@@ -496,10 +497,17 @@ extern "C" {
 
 int wah_server_create(uint64_t budget_bytes, uint32_t max_batch, uint32_t streams, int plain,
                       wah_server** out) {
+  return wah_server_create_tuned(budget_bytes, max_batch, streams, plain, 0, out);
+}
+
+int wah_server_create_tuned(uint64_t budget_bytes, uint32_t max_batch, uint32_t streams,
+                            int plain, int tuning, wah_server** out) {
   if (!out || budget_bytes == 0 || streams == 0 || streams > 8) return WAH_EINVAL;
   *out = nullptr;
+  if (tuning != 0 && !valid_tuning(tuning)) return WAH_EINVAL;
   wah_server* s = new (std::nothrow) wah_server;
   if (!s) return WAH_ENOMEM;
+  s->tuning = tuning;
   s->mode = plain ? 1 : 0;
   s->max_batch = plain ? 1 : std::max<uint32_t>(max_batch, 1);
   s->budget = arena_round(budget_bytes);

@@ -224,13 +224,84 @@ __device__ __forceinline__ void count_packed_keys(const uint32_t* __restrict__ w
     }
 }
 
-// Part q of a range: the rows one counting CTA covers (parts start on
-// multiples of 8 rows, so 16-byte loads of 32- and 16-bit keys stay aligned).
-__device__ __forceinline__ void sub_range(const RangeView& rv, uint32_t q, uint64_t* lo,
-                                          uint64_t* hi) {
-  const uint64_t part = ((rv.hi - rv.lo) / kCountCtasPerRange) & ~(uint64_t)7;
+// Key-start mode without packed words (columns whose pass-0 runs are short):
+// pass 0 wrote 16-bit keys in order of their low digit.  The same counts as
+// count_packed_keys, the low digit read from the key itself; 256-row chunks.
+__device__ __forceinline__ void histogram_range16_full(const uint16_t* __restrict__ keys,
+                                                       uint64_t lo, uint64_t hi,
+                                                       uint32_t (*s_h)[1][kRadix],
+                                                       uint32_t (*s_full)[kRadix],
+                                                       uint32_t* __restrict__ keyhist) {
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t nwarps = blockDim.x >> 5;
+  uint32_t* h1 = s_h[warp][0];    // digit-1 counts of the range
+  uint32_t* hw = s_full[warp];    // digit-1 counts for the warp's current low digit
+  uint32_t cur = kRadix;          // the low digit hw counts (none yet)
+  const uint4* kv = reinterpret_cast<const uint4*>(keys + lo);
+  const uint64_t chunks = (hi - lo) / 256;  // 32 lanes x 8 keys
+  auto add_chunk = [&](const uint4& q) {
+    const uint32_t k8[8] = {q.x & 0xFFFFu, q.x >> 16, q.y & 0xFFFFu, q.y >> 16,
+                            q.z & 0xFFFFu, q.z >> 16, q.w & 0xFFFFu, q.w >> 16};
+    const uint32_t first = __shfl_sync(0xffffffffu, k8[0], 0) & 0xFFu;
+    const uint32_t last = __shfl_sync(0xffffffffu, k8[7], 31) & 0xFFu;
+    if (first == last) {
+      if (first != cur) {
+        if (cur < kRadix) flush_keyhist(hw, h1, cur, lane, keyhist);
+        cur = first;
+      }
+#pragma unroll
+      for (int i = 0; i < 8; ++i) atomicAdd(&hw[k8[i] >> 8], 1u);
+    } else {
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        atomicAdd(&h1[k8[i] >> 8], 1u);
+        atomicAdd(&keyhist[k8[i]], 1u);
+      }
+    }
+  };
+  uint64_t c = warp;
+  for (; c + (kHistUnroll - 1) * nwarps < chunks; c += kHistUnroll * nwarps) {
+    uint4 q[kHistUnroll];
+#pragma unroll
+    for (int u = 0; u < kHistUnroll; ++u) q[u] = ld_stream_v4(kv + (c + u * nwarps) * 32 + lane);
+#pragma unroll
+    for (int u = 0; u < kHistUnroll; ++u) add_chunk(q[u]);
+  }
+  for (; c < chunks; c += nwarps) add_chunk(ld_stream_v4(kv + c * 32 + lane));
+  if (cur < kRadix) flush_keyhist(hw, h1, cur, lane, keyhist);
+  __syncwarp();
+  if (warp == 0)
+    for (uint64_t i = lo + chunks * 256 + lane; i < hi; i += 32) {
+      const uint32_t k = keys[i];
+      atomicAdd(&h1[k >> 8], 1u);
+      atomicAdd(&keyhist[k], 1u);
+    }
+}
+
+// Counting CTAs per range: two, or one where a one-column build's ranges
+// are short.
+template <class G>
+__device__ __forceinline__ uint32_t count_parts(const G& g) {
+  if constexpr (std::is_same<G, OneColumn>::value)
+    return g.count_parts ? g.count_parts : kCountCtasPerRange;
+  return kCountCtasPerRange;
+}
+
+// Part q of `parts` of a range: the rows one counting CTA covers (parts
+// start on multiples of 8 rows, so 16-byte loads of 32- and 16-bit keys stay
+// aligned).
+__device__ __forceinline__ void sub_range(const RangeView& rv, uint32_t q, uint32_t parts,
+                                          uint64_t* lo, uint64_t* hi) {
+  const uint64_t part = ((rv.hi - rv.lo) / parts) & ~(uint64_t)7;
   *lo = rv.lo + q * part;
-  *hi = q + 1 == kCountCtasPerRange ? rv.hi : *lo + part;
+  *hi = q + 1 == parts ? rv.hi : *lo + part;
+}
+
+// Adds one counting CTA's bin total to its copy of the bin totals.
+template <class G>
+__device__ __forceinline__ void add_bin_total(const G& g, int pass, uint32_t bin, uint32_t x) {
+  if constexpr (std::is_same<G, OneColumn>::value)
+    atomicAdd(&g.bintot[((blockIdx.x % kBinTotCopies) * kDigits + pass) * kRadix + bin], x);
 }
 
 // One read of the keys: per-range counts of digit 0, and the OR of the keys
@@ -242,11 +313,12 @@ __global__ void __launch_bounds__(kHistThreads)
   __shared__ uint32_t s_h[kHistWarps][1][kRadix];
   for (int i = threadIdx.x; i < kHistWarps * kRadix; i += kHistThreads) (&s_h[0][0][0])[i] = 0;
   __syncthreads();
-  const uint32_t r = blockIdx.x / kCountCtasPerRange;
+  const uint32_t parts = count_parts(g);
+  const uint32_t r = blockIdx.x / parts;
   const RangeView rv = g.range(r);
   const ColumnView c = g.col(rv.col);
   uint64_t lo, hi;
-  sub_range(rv, blockIdx.x % kCountCtasPerRange, &lo, &hi);
+  sub_range(rv, blockIdx.x % parts, parts, &lo, &hi);
   const uint2 acc = histogram_range<1>(c.input, lo, hi, 0, s_h);
   if ((threadIdx.x & 31) == 0) {
     if (acc.x) atomicOr(&c.ctrl->key_or, acc.x);
@@ -257,7 +329,10 @@ __global__ void __launch_bounds__(kHistThreads)
     uint32_t s = 0;
 #pragma unroll
     for (int w = 0; w < kHistWarps; ++w) s += s_h[w][0][j];
-    if (s) atomicAdd(&range_hist0[(uint64_t)r * kRadix + j], s);
+    if (s) {
+      atomicAdd(&range_hist0[(uint64_t)r * kRadix + j], s);
+      add_bin_total(g, 0, j, s);
+    }
   }
 }
 
@@ -265,7 +340,8 @@ __global__ void __launch_bounds__(kHistThreads)
 template <class G>
 __global__ void __launch_bounds__(kHistThreads)
     k_range_count(G g, int pass, uint32_t* __restrict__ range_hist) {
-  const uint32_t r = blockIdx.x / kCountCtasPerRange;
+  const uint32_t parts = count_parts(g);
+  const uint32_t r = blockIdx.x / parts;
   const RangeView rv = g.range(r);
   const ColumnView c = g.col(rv.col);
   const int src = c.ctrl->pass_src[pass];
@@ -274,7 +350,8 @@ __global__ void __launch_bounds__(kHistThreads)
   __shared__ uint32_t s_h[kHistWarps][1][kRadix];
   __shared__ uint32_t s_full[kHistWarps][kRadix];
   __shared__ uint32_t s_binoff[kRadix + 1];
-  const bool packed = c.ctrl->derive && pass == 1;  // key-start mode: packed pass-0 words
+  bool packed = false;  // key-start mode with packed pass-0 words
+  if constexpr (std::is_same<G, OneColumn>::value) packed = g.packed && c.ctrl->derive && pass == 1;
   for (int i = threadIdx.x; i < kHistWarps * kRadix; i += kHistThreads) {
     (&s_h[0][0][0])[i] = 0;
     (&s_full[0][0])[i] = 0;
@@ -287,10 +364,13 @@ __global__ void __launch_bounds__(kHistThreads)
   }
   __syncthreads();
   uint64_t lo, hi;
-  sub_range(rv, blockIdx.x % kCountCtasPerRange, &lo, &hi);
+  sub_range(rv, blockIdx.x % parts, parts, &lo, &hi);
   if (packed) {
     if constexpr (std::is_same<G, OneColumn>::value)
       count_packed_keys(keys, lo, hi, s_binoff, s_h, s_full, c.keyhist);
+  } else if (c.ctrl->derive && pass == 1) {  // 16-bit keys in low-digit order
+    histogram_range16_full(reinterpret_cast<const uint16_t*>(keys), lo, hi, s_h, s_full,
+                           c.keyhist);
   } else if (narrow_keys(c, src))
     histogram_range16<1>(reinterpret_cast<const uint16_t*>(keys), lo, hi, pass, s_h);
   else
@@ -300,7 +380,10 @@ __global__ void __launch_bounds__(kHistThreads)
     uint32_t s = 0;
 #pragma unroll
     for (int w = 0; w < kHistWarps; ++w) s += s_h[w][0][j];
-    if (s) atomicAdd(&range_hist[(uint64_t)r * kRadix + j], s);
+    if (s) {
+      atomicAdd(&range_hist[(uint64_t)r * kRadix + j], s);
+      add_bin_total(g, pass, j, s);
+    }
   }
 }
 
@@ -433,6 +516,28 @@ __global__ void __launch_bounds__(kRangeScanThreads)
     range_start[(uint64_t)c * kRadix + b] = run;
     run += range_hist[(uint64_t)c * kRadix + b];
   }
+}
+
+// One column: the same starts with one CTA per bin.  The bin's offset is
+// the sum of the totals of the smaller bins (kept by the count kernels), its
+// runs follow range by range (a scan of the bin's column of counts).
+constexpr int kRangeScanOneThreads = kMaxRanges;
+__global__ void __launch_bounds__(kRangeScanOneThreads)
+    k_range_scan_one(OneColumn g, int pass, const uint32_t* __restrict__ range_hist,
+                     uint32_t* __restrict__ range_start) {
+  __shared__ uint32_t s_warp[kRangeScanOneThreads / 32 + 1];
+  if (g.c.ctrl->pass_src[pass] < 0) return;
+  const uint32_t b = blockIdx.x, t = threadIdx.x;
+  uint32_t tot = 0;  // bin t's total: the sum of its copies
+  if (t < b)
+#pragma unroll
+    for (int k = 0; k < kBinTotCopies; ++k) tot += g.bintot[(k * kDigits + pass) * kRadix + t];
+  uint32_t below;
+  block_exclusive_scan<kRangeScanOneThreads>(tot, &below, s_warp);
+  const uint32_t x = t < g.ranges ? range_hist[(uint64_t)t * kRadix + b] : 0u;
+  uint32_t all;
+  const uint32_t pre = block_exclusive_scan<kRangeScanOneThreads>(x, &all, s_warp);
+  if (t < g.ranges) range_start[(uint64_t)t * kRadix + b] = below + pre;
 }
 
 // ---------------------------------------------------------------------------
@@ -903,7 +1008,7 @@ __global__ void __launch_bounds__(kSortThreads, ITEMS <= 12 ? 3 : 2)
   const int src = col.ctrl->pass_src[pass];
   if (src < 0) return;  // trivial digit: every row in one bin, order unchanged
   if constexpr (std::is_same<G, OneColumn>::value) {
-    if (col.ctrl->derive) {  // key-start mode: passes 0 and 1 exchange packed words
+    if (g.packed && col.ctrl->derive) {  // key-start mode: passes 0 and 1 exchange packed words
       if (pass == 0) scatter_pack0<ITEMS, PEERS>(g, range_start, smem_raw);
       else scatter_pack1<ITEMS, PEERS>(g, range_start, smem_raw);
       return;
@@ -1081,9 +1186,17 @@ cudaError_t launch_sort_t(const G& g0, uint32_t ranges0, const SortVariant<G>& v
                           uint32_t ranges1, const SortVariant<G>& v1, uint32_t ncols,
                           const RangeArrays& ra, const LaunchOpts& o, cudaStream_t s,
                           uint32_t* launches) {
-  const unsigned count_grid = ranges0 * kCountCtasPerRange;
-  cudaError_t err =
-      cudaMemsetAsync(ra.hist, 0, (size_t)kDigits * ra.max_ranges * kRadix * 4, s);
+  uint32_t parts0 = kCountCtasPerRange, parts1 = kCountCtasPerRange;
+  if constexpr (std::is_same<G, OneColumn>::value) {
+    if (g0.count_parts) parts0 = g0.count_parts;
+    if (g1.count_parts) parts1 = g1.count_parts;
+  }
+  const unsigned count_grid = ranges0 * parts0;
+  // the per-range histograms (and, for one column, the bin totals after them)
+  cudaError_t err = cudaMemsetAsync(
+      ra.hist, 0,
+      ((size_t)kDigits * ra.max_ranges + (ra.bintot ? kBinTotCopies * kDigits : 0)) * kRadix * 4,
+      s);
   if (err != cudaSuccess) return err;
   record_phase(o.events, kPhaseHist, false, s);
   k_digit_histogram<G><<<count_grid, kHistThreads, 0, s>>>(g0, ra.hist);
@@ -1109,7 +1222,7 @@ cudaError_t launch_sort_t(const G& g0, uint32_t ranges0, const SortVariant<G>& v
     const SortVariant<G>& v = p == 0 ? v0 : v1;
     record_phase(o.events, kPhasePass0 + p, false, s);
     if (p > 0) {
-      k_range_count<G><<<ranges * kCountCtasPerRange, kHistThreads, 0, s>>>(gp, p, rh);
+      k_range_count<G><<<ranges * (p == 0 ? parts0 : parts1), kHistThreads, 0, s>>>(gp, p, rh);
       ++*launches;
     }
     if constexpr (std::is_same<G, OneColumn>::value) {
@@ -1118,7 +1231,10 @@ cudaError_t launch_sort_t(const G& g0, uint32_t ranges0, const SortVariant<G>& v
         ++*launches;
       }
     }
-    k_range_scan<G><<<ncols, kRangeScanThreads, 0, s>>>(gp, p, rh, ra.start);
+    if constexpr (std::is_same<G, OneColumn>::value)
+      k_range_scan_one<<<kRadix, kRangeScanOneThreads, 0, s>>>(gp, p, rh, ra.start);
+    else
+      k_range_scan<G><<<ncols, kRangeScanThreads, 0, s>>>(gp, p, rh, ra.start);
     ++*launches;
     record_phase(o.events, kPhaseScatter0 + p, false, s);
     v.fn<<<ranges, kSortThreads, v.smem, s>>>(gp, p, ra.start);
@@ -1137,12 +1253,13 @@ static OneColumn one_column_ranges(const ColumnView& c, const SortVariant<OneCol
                                    int per_sm, const RangeArrays& ra, const LaunchOpts& o) {
   uint64_t want = (uint64_t)std::max(o.sm_count, 1) * std::max(per_sm, 1);
   if (want > ra.max_ranges) want = ra.max_ranges;
-  const uint64_t tile = (uint64_t)kSortThreads * v.items;
-  const uint64_t quantum = std::lcm<uint64_t>(tile, kRangeQuantum);
+  // ranges of whole tiles (a column's last range may end inside a tile)
+  const uint64_t quantum = (uint64_t)kSortThreads * v.items;
   OneColumn g{};
   g.c = c;
   g.range_rows = std::max<uint64_t>(ceil_div(ceil_div(c.n, want), quantum) * quantum, quantum);
   g.ranges = (uint32_t)std::max<uint64_t>(ceil_div(c.n, g.range_rows), 1);
+  g.count_parts = g.range_rows < 32768 ? 1 : kCountCtasPerRange;  // short ranges: one CTA
   return g;
 }
 
@@ -1161,8 +1278,12 @@ cudaError_t launch_sort_one(const ColumnView& c, const RangeArrays& ra, const La
   OneColumn g0 = one_column_ranges(c, v0, per_sm0, ra, o);
   OneColumn g1 = one_column_ranges(c, v1, per_sm1, ra, o);
   // Key-start mode packs a row's offset in its pass-0 range into 24 bits and
-  // needs the table of pass-0 runs.
-  if (!ra.seg0 || g0.range_rows >= kPackRangeRows) g0.c.derive_ok = g1.c.derive_ok = 0;
+  // needs the table of pass-0 runs; it pays where those runs are long (each
+  // pass-1 warp slice then mostly lies inside one run), else the 16-bit keys
+  // go between the passes.
+  g0.packed = g1.packed = ra.seg0 && g0.range_rows < kPackRangeRows &&
+                          (o.pack_force || g0.range_rows >= kPackMinRangeRows);
+  g0.bintot = g1.bintot = ra.bintot;
   g0.ranges0 = g1.ranges0 = g0.ranges;
   g0.range_rows0 = g1.range_rows0 = g0.range_rows;
   g0.seg0 = g1.seg0 = ra.seg0;

@@ -73,9 +73,24 @@ def test_tuning_encoding(lib):
             assert lib.wah_set_tuning(good) == 0, good
             assert lib.wah_get_tuning() == good
         cur = lib.wah_get_tuning()
-        for bad in (0, 7, 20, 16 | 0x300, 16 | 0x400, 16 | (7 << 16), 16 | (0x200 << 16),
+        for bad in (0, 7, 20, 16 | 0x300, 16 | 0x800, 16 | (7 << 16), 16 | (0x200 << 16),
                     16 | ((12 | 0x300) << 16), -1):
             assert lib.wah_set_tuning(bad) == 1, bad  # WAH_EINVAL
             assert lib.wah_get_tuning() == cur
     finally:
         lib.wah_set_tuning(old)
+
+
+def test_tuning_words_are_validated_on_the_host(lib):
+    """Tuning words: rows per thread 8/12/16, one peer mode, the packed flag
+    only in the first shape; a bad word is refused before any device work."""
+    before = lib.wah_get_tuning()
+    for bad in (0, -1, 7, 16 | 0x300, 16 | ((12 | 0x400) << 16), 16 | 0x800, 16 | (5 << 16)):
+        assert lib.wah_set_tuning(bad) == 1, bad
+        if bad != 0:  # 0 in a call means the process default
+            assert lib.wah_build_tuned(None, 1000, 0, None, None, None, ctypes.c_void_p(16), None,
+                                       0, bad, None) == 1, bad
+    assert lib.wah_get_tuning() == before
+    for good in (16, 12 | 0x100, 8 | 0x200 | 0x400, 16 | 0x200 | ((12 | 0x200) << 16)):
+        assert lib.wah_set_tuning(good) == 0, good
+    lib.wah_set_tuning(before)

@@ -191,7 +191,7 @@ def test_rejects_unknown_tuning(wah):
     lib = wah._lib.load()
     old = lib.wah_get_tuning()
     for bad in (7, 20, 16 | 0x300, 16 | later(7), 16 | later(12 | 0x300), 16 | later(0x200),
-                -1):
+                16 | later(12 | 0x400), 16 | 0x800, 0, -1):
         assert lib.wah_set_tuning(bad) == wah.WAH_EINVAL, bad
     assert lib.wah_get_tuning() == old
 
