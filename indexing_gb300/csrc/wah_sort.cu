@@ -896,6 +896,7 @@ __device__ __forceinline__ void scatter_pack1(const OneColumn& g,
   // every warp: the run holding the range's first row (seg0[0] = 0 <= lo)
   uint32_t i0 = warp_count_le(seg0, nseg, (uint32_t)lo) - 1;
   uint32_t ent = i0 + 1 + lane < nseg ? seg0[i0 + 1 + lane] : 0xffffffffu;  // run starts i0+1..
+  uint32_t rmod = (i0 + lane) % r0;  // range of run i0 + lane, followed as i0 advances
   __syncthreads();
 
   const uint32_t row0 = warp * SLICE + lane;
@@ -932,11 +933,17 @@ __device__ __forceinline__ void scatter_pack1(const OneColumn& g,
       const uint32_t k0 = __popc(__ballot_sync(0xffffffffu, ent <= s0));
       const uint32_t k1 = __popc(__ballot_sync(0xffffffffu, ent < s1));
       if (k1 < 32) {
-        const uint32_t mybase = ((i0 + lane) % r0) * rows0;  // first row id of run i0 + lane
+        const uint32_t mybase = rmod * rows0;  // first row id of run i0 + lane
         const uint32_t b0 = __shfl_sync(0xffffffffu, mybase, k0);
         if (k1 == k0) {
 #pragma unroll
           for (int j = 0; j < ITEMS; ++j) rid[j] = b0 + (word[j] >> 8);
+        } else if (k1 == k0 + 1) {  // one run starts inside the slice
+          const uint32_t bnd = __shfl_sync(0xffffffffu, ent, k0);
+          const uint32_t b1 = __shfl_sync(0xffffffffu, mybase, k0 + 1);
+#pragma unroll
+          for (int j = 0; j < ITEMS; ++j)
+            rid[j] = (s0 + lane + j * 32 >= bnd ? b1 : b0) + (word[j] >> 8);
         } else {
 #pragma unroll
           for (int j = 0; j < ITEMS; ++j) {
@@ -958,7 +965,14 @@ __device__ __forceinline__ void scatter_pack1(const OneColumn& g,
       if (i + 1 < ntiles) {
         const uint32_t p_next = (uint32_t)(base + TILE);
         const uint32_t adv = __popc(__ballot_sync(0xffffffffu, ent <= p_next));
-        i0 = adv < 32 ? i0 + adv : warp_count_le(seg0, nseg, p_next) - 1;
+        if (adv < 32) {
+          i0 += adv;
+          rmod += adv;
+          while (rmod >= r0) rmod -= r0;
+        } else {
+          i0 = warp_count_le(seg0, nseg, p_next) - 1;
+          rmod = (i0 + lane) % r0;
+        }
         ent = i0 + 1 + lane < nseg ? seg0[i0 + 1 + lane] : 0xffffffffu;
       }
     }
