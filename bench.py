@@ -1253,9 +1253,9 @@ def main():
     # DRAM bytes per row of each kernel (dram__bytes_read.sum +
     # dram__bytes_write.sum, one ncu capture of a 67,108,864-row uniform
     # 16-bit column with the same tile shape); traffic grows with rows.
-    traffic_per_row = {"histogram": 4.05, "scatter0": 13.03, "scatter1": 11.05, "emit": 11.28}
+    traffic_per_row = {"histogram": 4.05, "scatter0": 8.85, "scatter1": 8.91, "emit": 11.29}
     # DRAM bytes per row of each phase (every kernel of it), same capture
-    phase_dram_per_row = {"histogram": 4.05, "pass0": 13.03, "pass1": 13.19, "build": 15.45}
+    phase_dram_per_row = {"histogram": 4.05, "pass0": 8.86, "pass1": 13.05, "build": 15.46}
     dram_bytes = (sum(phase_dram_per_row.values()) * n
                   if card == 65536 and derive else None)
     per_unit = {"histogram": "4 B/row",
@@ -1426,7 +1426,8 @@ def main():
                          "frac": ach / peak, "peak_kind": peak_kind,
                          "traffic": (traffic_per_row[dom] * n
                                      if card == 65536 and dom in traffic_per_row else None),
-                         "traffic_source": "ncu capture at 67,108,864 rows, scaled by rows"},
+                         "traffic_source": "ncu capture at 67,108,864 rows (12-row tiles in "
+                                           "both digit passes), scaled by rows"},
             "gpu_launches": launches,
             "clocks": cl,
             "e2e": e2e,

@@ -40,14 +40,16 @@ extern "C" {
 #define WAH_ENOMEM 2    /* workspace too small / allocation failed          */
 #define WAH_ECUDA 3     /* a CUDA runtime call failed                       */
 #define WAH_ETIMEOUT 4  /* a bounded device-side wait gave up               */
-#define WAH_ERANGE 5    /* n >= 2^30, or a value above the stated bound     */
+#define WAH_ERANGE 5    /* n >= 2^31, or a value above the stated bound     */
 #define WAH_EOVERFLOW 6 /* an output would exceed the caller's capacity     */
 #define WAH_ENODEV 7    /* no usable sm_103 device                          */
 #define WAH_ECORRUPT 8  /* index words do not describe the stated rows      */
 
 /* Largest column one call accepts (rows).  Offsets and index positions are
- * u32 as in the reference; n < 2^30 keeps every counter in range. */
-#define WAH_MAX_ROWS ((uint64_t)1 << 30)
+ * u32 as in the reference (src/cpu.cpp:261-272); with n < 2^31 rows a
+ * column's index holds L <= 2n < 2^32 words, so every row, word and key
+ * position stays within u32. */
+#define WAH_MAX_ROWS ((uint64_t)1 << 31)
 
 /* Device-written result counters (16 bytes). */
 typedef struct wah_counts {

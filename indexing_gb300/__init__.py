@@ -44,7 +44,7 @@ __all__ = ["WahError", "WahIndex", "build_index", "sort_rids_by_value", "build_s
            "TUNE_MATCH", "TUNE_HYBRID", "TUNE_PACK", "WORKLOAD_UNIFORM", "WORKLOAD_SKEWED",
            "WORKLOAD_BATCH"]
 
-MAX_ROWS = 1 << 30
+MAX_ROWS = 1 << 31
 
 WAH_OK, WAH_EINVAL, WAH_ENOMEM, WAH_ECUDA, WAH_ETIMEOUT, WAH_ERANGE, WAH_EOVERFLOW, \
     WAH_ENODEV, WAH_ECORRUPT = range(9)

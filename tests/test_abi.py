@@ -57,8 +57,8 @@ def test_output_caps_and_workspace(lib):
 
 
 def test_rejects_oversize_without_touching_device(lib):
-    # n >= 2^30 is refused before any CUDA call
-    rc = lib.wah_build(None, 1 << 30, 0, None, None, None, ctypes.c_void_p(16), None, 0, None)
+    # n >= 2^31 is refused before any CUDA call
+    rc = lib.wah_build(None, 1 << 31, 0, None, None, None, ctypes.c_void_p(16), None, 0, None)
     assert rc == 5
 
 

@@ -212,10 +212,11 @@ def test_query_output_capacity_is_reported(wah):
 
 
 def test_largest_column(wah):
-    """The largest column one call accepts, 2^30 - 1 rows (every word
-    position stays within u32): built and decoded back to the column bit for
-    bit on the GPU; 2^30 rows are refused with WAH_ERANGE before any work."""
-    n = (1 << 30) - 1
+    """The largest column one call accepts, 2^31 - 1 rows (every row, word
+    and key position stays within u32: L <= 2n < 2^32): built and decoded back
+    to the column bit for bit on the GPU; 2^31 rows are refused with
+    WAH_ERANGE before any work."""
+    n = (1 << 31) - 1
     g = torch.Generator(device="cuda")
     g.manual_seed(30)
     col = torch.randint(0, 65536, (n,), device="cuda", dtype=torch.int32, generator=g)
@@ -228,10 +229,10 @@ def test_largest_column(wah):
     assert int(starts[0].item()) == 0 and bool((starts[1:] > starts[:-1]).all())
     del d, idx, starts
     torch.cuda.empty_cache()
-    # 2^30 rows through the C ABI: refused before anything is read or written
+    # 2^31 rows through the C ABI: refused before anything is read or written
     lib = wah._lib.load()
     counts = torch.zeros(4, dtype=torch.int32, device="cuda")
     dummy = torch.zeros(4, dtype=torch.int32, device="cuda")
     p = dummy.data_ptr()
-    rc = lib.wah_build(p, 1 << 30, 65535, p, p, p, counts.data_ptr(), p, 16, None)
+    rc = lib.wah_build(p, 1 << 31, 65535, p, p, p, counts.data_ptr(), p, 16, None)
     assert rc == wah.WAH_ERANGE

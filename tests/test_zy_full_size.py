@@ -13,7 +13,8 @@ restatement of the reference `cpu` program, run on host threads:
 * the 20,000-request serving trace: every request served in the mix equals
   the same request built alone (a 64-bit fingerprint of its keys, offsets
   and index, taken on the device), and a seeded sample equals the oracle
-  word for word.
+  word for word;
+* a column of 2^30 + 4,099 rows, above the row limit of earlier builds.
 
 The inputs come from the benchmark's own generators.  The file name makes
 pytest collect it after the other GPU tests and before the allocation-free
@@ -112,3 +113,18 @@ def test_serving_trace_each_request_equal_alone(env):
     assert out["equal_alone"] == nreq, f"differ from alone: {out['differ_alone'][:10]}"
     assert out["oracle_checked"] == 64
     assert not out["oracle_differ"], f"differ from the oracle: {out['oracle_differ']}"
+
+
+def test_column_above_two_to_the_thirty(env):
+    """A column just above 2^30 rows (the limit before u32 positions were
+    shown to hold up to 2^31 rows), against the oracle word for word."""
+    wah, lib, dev = env
+    n = (1 << 30) + 4099
+    v = bench.gen_uniform(n, 65536, SEED + 30)
+    d = torch.from_numpy(v.view(np.int32)).to(dev)
+    got = _build(lib, wah, d, n, 65535, dev)
+    del d
+    torch.cuda.empty_cache()
+    assert got[0] == 0
+    bad, count = bench.check_columns([(v, got)], 1)
+    assert count == 1 and not bad
