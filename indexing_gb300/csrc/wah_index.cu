@@ -251,6 +251,7 @@ struct EmitSmem {
   uint32_t keys[kSkewed(kBuildTile)];
   uint32_t offs[kSkewed(kBuildTile)];
   uint32_t warp_tot[kBuildThreads / 32];  // the warps' packed (words, keys) totals
+  uint64_t red[3 * (kBuildThreads / 32)];  // one column: the range-start sums
   uint64_t bar[2];
   int abort;
 };
@@ -280,6 +281,56 @@ __device__ __forceinline__ void fetch_window(uint32_t* wv, uint32_t* wr, uint64_
   if (sr) bulk_copy_g2s(wr, sr + base - kWinBehind, bytes, bar);
 }
 
+// One column: range r's first word and key are the sums of the word and key
+// counts of ranges 0 .. r-1, summed by the emit CTA itself instead of a
+// separate scan launch; CTA 0 also sums every range and writes the column's
+// totals (the index length, the key count, the merged entries).
+__device__ __forceinline__ void own_range_start(const OneColumn& g,
+                                                const uint32_t* __restrict__ counts,
+                                                uint32_t* run_w, uint32_t* run_k,
+                                                uint64_t* s_red) {
+  const uint32_t r = blockIdx.x, nr = g.ranges;
+  const uint32_t lim = r == 0 ? nr : r;
+  uint64_t mine = 0, all = 0, segs = 0;
+  for (uint32_t i = threadIdx.x; i < lim; i += kBuildThreads) {
+    const uint4 c = reinterpret_cast<const uint4*>(counts)[i];
+    const uint64_t x = ((uint64_t)c.y << 32) | c.x;  // keys, words
+    all += x;
+    segs += c.z;
+    if (i < r) mine += x;
+  }
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) {
+    mine += __shfl_xor_sync(0xffffffffu, mine, d);
+    all += __shfl_xor_sync(0xffffffffu, all, d);
+    segs += __shfl_xor_sync(0xffffffffu, segs, d);
+  }
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  constexpr int NW = kBuildThreads / 32;
+  if (lane == 0) {
+    s_red[warp] = mine;
+    s_red[NW + warp] = all;
+    s_red[2 * NW + warp] = segs;
+  }
+  __syncthreads();
+  uint64_t m = 0, a = 0, sg = 0;
+#pragma unroll
+  for (int w = 0; w < NW; ++w) {
+    m += s_red[w];
+    a += s_red[NW + w];
+    sg += s_red[2 * NW + w];
+  }
+  *run_w = (uint32_t)(m & 0xffffffffu);
+  *run_k = (uint32_t)(m >> 32);
+  if (r == 0 && threadIdx.x == 0) {
+    const ColumnView& col = g.col(0);
+    col.counts->index_len = (uint32_t)(a & 0xffffffffu);
+    col.counts->keycnt = (uint32_t)(a >> 32);
+    col.counts->merged = (uint32_t)sg;
+  }
+  __syncthreads();
+}
+
 // kDerive: key heads from the key-start bits, keys written already (derive
 // mode, one column only)
 template <class G, bool kDerive>
@@ -303,8 +354,14 @@ __device__ __forceinline__ void build_emit(const G& g, const uint32_t* __restric
   const uint64_t lo = rv.lo, hi = rv.hi;
   if (lo >= hi) return;
   const uint32_t ntiles = (uint32_t)ceil_div(hi - lo, kBuildTile);
-  uint32_t run_w = range_first[blockIdx.x * 2 + 0];  // words before this tile
-  uint32_t run_k = range_first[blockIdx.x * 2 + 1];  // keys before this tile
+  uint32_t run_w, run_k;  // words and keys before this tile
+  if constexpr (std::is_same<G, OneColumn>::value) {
+    // range_first holds the per-range counts here
+    own_range_start(g, range_first, &run_w, &run_k, sm.red);
+  } else {
+    run_w = range_first[blockIdx.x * 2 + 0];
+    run_k = range_first[blockIdx.x * 2 + 1];
+  }
 
   if (tid == 0) {
     mbar_init(&sm.bar[0], 1);
@@ -546,12 +603,16 @@ cudaError_t launch_build_t(const G& g, uint32_t ncols, uint32_t ranges, const Ra
   if (err != cudaSuccess) return err;
   record_phase(o.events, kPhaseBuild, false, s);
   k_build_count<G><<<ranges * kCountCtasPerRange, kHistThreads, 0, s>>>(g, ra.counts);
-  k_build_scan<G><<<ncols, kBuildScanThreads, 0, s>>>(g, ra.counts, ra.first);
+  if constexpr (!std::is_same<G, OneColumn>::value) {  // one column: inside the emit
+    k_build_scan<G><<<ncols, kBuildScanThreads, 0, s>>>(g, ra.counts, ra.first);
+    ++*launches;
+  }
   record_phase(o.events, kPhaseEmit, false, s);
-  k_build_emit<G><<<ranges, kBuildThreads, smem, s>>>(g, ra.first);
+  k_build_emit<G><<<ranges, kBuildThreads, smem, s>>>(
+      g, std::is_same<G, OneColumn>::value ? ra.counts : ra.first);
   record_phase(o.events, kPhaseEmit, true, s);
   record_phase(o.events, kPhaseBuild, true, s);
-  *launches += 3;
+  *launches += 2;
   return cudaGetLastError();
 }
 

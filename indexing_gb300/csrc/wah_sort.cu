@@ -390,38 +390,49 @@ __global__ void __launch_bounds__(kHistThreads)
 // ---------------------------------------------------------------------------
 // Pass plan: bin offsets per digit, trivial digits skipped, ping-pong homes.
 // ---------------------------------------------------------------------------
-template <class G>
-__global__ void __launch_bounds__(kRadix) k_sort_plan(G g) {
-  const ColumnView c = g.col(blockIdx.x);
+// The plan of one column from the OR of its keys and of their complements;
+// written to ctrl when `write`, and returns the source of digit pass 0
+// (-1: trivial).
+__device__ __forceinline__ int plan_column(const ColumnView& c, bool write) {
   WahCtrl* ctrl = c.ctrl;
   const int passes = c.passes;
-  uint32_t* status = c.status;
-  if (threadIdx.x == 0) {
-    // a digit every key shares is trivial: one bin, order unchanged
-    const uint32_t varying = ctrl->key_or & ctrl->key_nor;
-    int s_active[kDigits];
-    for (int p = 0; p < kDigits; ++p) s_active[p] = digit8(varying, p) != 0;
+  const uint32_t key_or = ctrl->key_or;
+  // a digit every key shares is trivial: one bin, order unchanged
+  const uint32_t varying = key_or & ctrl->key_nor;
+  int s_active[kDigits];
+  for (int p = 0; p < kDigits; ++p) s_active[p] = digit8(varying, p) != 0;
+  int src0 = -1;
+  if (write) {
     // every key below 2^16 (digits 2 and 3 then inactive): 16-bit keys
     // between the passes, and key starts when both low digits vary
-    ctrl->narrow = (ctrl->key_or >> 16) == 0;
+    ctrl->narrow = (key_or >> 16) == 0;
     ctrl->derive = c.derive_ok && ctrl->narrow && s_active[0] && s_active[1];
     // A set bit above the digits the bound allows: the sort would be wrong.
-    if (passes < kDigits && (ctrl->key_or >> (passes * kRadixBits)) != 0)
-      set_status(status, WAH_ERANGE);
-    int cur = kSelInput;
-    for (int p = 0; p < kDigits; ++p) {
-      if (p < passes && s_active[p]) {
-        ctrl->pass_src[p] = cur;
-        const int dst = (cur == kSelA) ? kSelB : kSelA;
-        ctrl->pass_dst[p] = dst;
-        cur = dst;
-      } else {
-        ctrl->pass_src[p] = -1;
-        ctrl->pass_dst[p] = -1;
-      }
-    }
-    ctrl->final_sel = cur;
+    if (passes < kDigits && (key_or >> (passes * kRadixBits)) != 0)
+      set_status(c.status, WAH_ERANGE);
   }
+  int cur = kSelInput;
+  for (int p = 0; p < kDigits; ++p) {
+    if (p < passes && s_active[p]) {
+      const int dst = (cur == kSelA) ? kSelB : kSelA;
+      if (p == 0) src0 = cur;
+      if (write) {
+        ctrl->pass_src[p] = cur;
+        ctrl->pass_dst[p] = dst;
+      }
+      cur = dst;
+    } else if (write) {
+      ctrl->pass_src[p] = -1;
+      ctrl->pass_dst[p] = -1;
+    }
+  }
+  if (write) ctrl->final_sel = cur;
+  return src0;
+}
+
+template <class G>
+__global__ void __launch_bounds__(kRadix) k_sort_plan(G g) {
+  if (threadIdx.x == 0) plan_column(g.col(blockIdx.x), true);
 }
 
 // Key starts (derive mode): keyhist scanned in key order; the first row of
@@ -433,11 +444,10 @@ constexpr int kKeyStartThreads = 1024;
 constexpr int kKeyStartCtas = 65536 / kKeyStartThreads;
 
 template <class G>
-__global__ void __launch_bounds__(kKeyStartThreads) k_key_starts(G g) {
-  __shared__ uint64_t s_warp[kKeyStartThreads / 32 + 1];
+__device__ __forceinline__ void key_starts(const G& g, uint32_t block, uint64_t* s_warp) {
   const ColumnView c = g.col(0);
   if (!c.ctrl->derive) return;
-  const uint32_t k0 = blockIdx.x * kKeyStartThreads;
+  const uint32_t k0 = block * kKeyStartThreads;
   const uint4* kh4 = reinterpret_cast<const uint4*>(c.keyhist);
   uint64_t below = 0;
 #pragma unroll 4
@@ -460,6 +470,12 @@ __global__ void __launch_bounds__(kKeyStartThreads) k_key_starts(G g) {
   else set_status(c.status, WAH_ECORRUPT);
   if (rank < c.keys_cap) c.keys[rank] = key;
   else set_status(c.status, WAH_EOVERFLOW);
+}
+
+template <class G>
+__global__ void __launch_bounds__(kKeyStartThreads) k_key_starts(G g) {
+  __shared__ uint64_t s_warp[kKeyStartThreads / 32 + 1];
+  key_starts(g, blockIdx.x, s_warp);
 }
 
 // Start of every (range, bin) of one column for one pass: the bin's offset
@@ -521,12 +537,37 @@ __global__ void __launch_bounds__(kRangeScanThreads)
 // One column: the same starts with one CTA per bin.  The bin's offset is
 // the sum of the totals of the smaller bins (kept by the count kernels), its
 // runs follow range by range (a scan of the bin's column of counts).
+// The same launch also does the column's plan (digit pass 0: every CTA
+// derives it from the key OR and NOR, CTA 0 writes it) and, for digit pass
+// 1, the key starts (kKeyStartCtas more CTAs after the 256 bin CTAs): two
+// launches fewer per build, which counts for small columns.
 constexpr int kRangeScanOneThreads = kMaxRanges;
+static_assert(kKeyStartThreads == kRangeScanOneThreads, "key-start CTAs share the launch");
 __global__ void __launch_bounds__(kRangeScanOneThreads)
     k_range_scan_one(OneColumn g, int pass, const uint32_t* __restrict__ range_hist,
                      uint32_t* __restrict__ range_start) {
   __shared__ uint32_t s_warp[kRangeScanOneThreads / 32 + 1];
-  if (g.c.ctrl->pass_src[pass] < 0) return;
+  __shared__ uint64_t s_warp64[kRangeScanOneThreads / 32 + 1];
+  if (blockIdx.x >= kRadix) {  // digit pass 1: the key starts
+    key_starts(g, blockIdx.x - kRadix, s_warp64);
+    return;
+  }
+  if (pass == 0) {
+    // key-start mode's key counts and bits start at zero (first used by the
+    // count before digit pass 1); the 256 CTAs clear them with 16-byte stores
+    if (g.c.derive_ok && g.c.passes >= 2) {
+      const uint64_t stride = (uint64_t)gridDim.x * kRangeScanOneThreads;
+      const uint64_t t = (uint64_t)blockIdx.x * kRangeScanOneThreads + threadIdx.x;
+      uint4* kh = reinterpret_cast<uint4*>(g.c.keyhist);
+      for (uint64_t i = t; i < 65536 / 4; i += stride) kh[i] = make_uint4(0, 0, 0, 0);
+      uint4* ks = reinterpret_cast<uint4*>(g.c.keystart);  // n/32 words + 16 of slack
+      const uint64_t q = ceil_div(ceil_div(g.c.n, 32), 4);
+      for (uint64_t i = t; i < q; i += stride) ks[i] = make_uint4(0, 0, 0, 0);
+    }
+    if (plan_column(g.c, blockIdx.x == 0 && threadIdx.x == 0) < 0) return;
+  } else if (g.c.ctrl->pass_src[pass] < 0) {
+    return;
+  }
   const uint32_t b = blockIdx.x, t = threadIdx.x;
   uint32_t tot = 0;  // bin t's total: the sum of its copies
   if (t < b)
@@ -1217,9 +1258,11 @@ cudaError_t launch_sort_t(const G& g0, uint32_t ranges0, const SortVariant<G>& v
   record_phase(o.events, kPhaseHist, true, s);
   ++*launches;
   record_phase(o.events, kPhasePlan, false, s);
-  k_sort_plan<G><<<ncols, kRadix, 0, s>>>(g0);
+  if constexpr (!std::is_same<G, OneColumn>::value) {  // one column: in the pass-0 range scan
+    k_sort_plan<G><<<ncols, kRadix, 0, s>>>(g0);
+    ++*launches;
+  }
   record_phase(o.events, kPhasePlan, true, s);
-  ++*launches;
   err = cudaGetLastError();
   if (err != cudaSuccess) return err;
   for (int p = 0; p < kDigits; ++p) {
@@ -1239,14 +1282,9 @@ cudaError_t launch_sort_t(const G& g0, uint32_t ranges0, const SortVariant<G>& v
       k_range_count<G><<<ranges * (p == 0 ? parts0 : parts1), kHistThreads, 0, s>>>(gp, p, rh);
       ++*launches;
     }
-    if constexpr (std::is_same<G, OneColumn>::value) {
-      if (p == 1 && gp.c.derive_ok) {  // works only in derive mode
-        k_key_starts<G><<<kKeyStartCtas, kKeyStartThreads, 0, s>>>(gp);
-        ++*launches;
-      }
-    }
-    if constexpr (std::is_same<G, OneColumn>::value)
-      k_range_scan_one<<<kRadix, kRangeScanOneThreads, 0, s>>>(gp, p, rh, ra.start);
+    if constexpr (std::is_same<G, OneColumn>::value)  // + the key starts for digit pass 1
+      k_range_scan_one<<<kRadix + (p == 1 && gp.c.derive_ok ? kKeyStartCtas : 0),
+                         kRangeScanOneThreads, 0, s>>>(gp, p, rh, ra.start);
     else
       k_range_scan<G><<<ncols, kRangeScanThreads, 0, s>>>(gp, p, rh, ra.start);
     ++*launches;
@@ -1301,11 +1339,6 @@ cudaError_t launch_sort_one(const ColumnView& c, const RangeArrays& ra, const La
   g0.ranges0 = g1.ranges0 = g0.ranges;
   g0.range_rows0 = g1.range_rows0 = g0.range_rows;
   g0.seg0 = g1.seg0 = ra.seg0;
-  if (g0.c.derive_ok && c.passes >= 2) {  // key counts and key starts (derive mode)
-    err = cudaMemsetAsync(c.keyhist, 0, (size_t)65536 * 4, s);
-    if (err == cudaSuccess) err = cudaMemsetAsync(c.keystart, 0, ceil_div(c.n, 32) * 4, s);
-    if (err != cudaSuccess) return err;
-  }
   return launch_sort_t<OneColumn>(g0, g0.ranges, v0, g1, g1.ranges, v1, 1, ra, o, s, launches);
 }
 
