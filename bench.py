@@ -1253,9 +1253,9 @@ def main():
     # DRAM bytes per row of each kernel (dram__bytes_read.sum +
     # dram__bytes_write.sum, one ncu capture of a 67,108,864-row uniform
     # 16-bit column with the same tile shape); traffic grows with rows.
-    traffic_per_row = {"histogram": 4.05, "scatter0": 8.85, "scatter1": 8.91, "emit": 11.29}
+    traffic_per_row = {"histogram": 4.05, "scatter0": 8.85, "scatter1": 8.87, "emit": 11.28}
     # DRAM bytes per row of each phase (every kernel of it), same capture
-    phase_dram_per_row = {"histogram": 4.05, "pass0": 8.86, "pass1": 13.05, "build": 15.46}
+    phase_dram_per_row = {"histogram": 4.05, "pass0": 8.86, "pass1": 13.02, "build": 15.45}
     dram_bytes = (sum(phase_dram_per_row.values()) * n
                   if card == 65536 and derive else None)
     per_unit = {"histogram": "4 B/row",
