@@ -1222,26 +1222,42 @@ def main():
 
     # Algorithmic bytes per build: histogram 4n; digit pass 0 12n (read key,
     # write key + rid), later passes 16n -- with two passes the key between
-    # them is 16-bit: pass 0 10n, pass 1 14n (2 + 4 in, 4 + 4 out); build
-    # 8n + 4L + 8K (read sorted key + rid, write words, keys, offsets).  When
-    # both digits of a two-pass column vary (key-start mode), pass 0 writes
-    # one packed word per row (row offset in its range and high digit: 8n),
-    # the pass-1 count reads those words (4n), pass 1 reads them and writes
-    # row ids and the key-start bits (8n + n/8), and the build reads row ids
-    # and bits (4n + n/8 + 4L + 8K).  A phase (count + scan + kernel) and its
-    # main kernel are credited the same bytes, except the pass-1 count; the
-    # roofline is taken on the longest single kernel.
+    # them is 16-bit: pass 0 10n, pass 1 14n (2 + 4 in, 4 + 4 out); emit
+    # 8n + 4L + 8K (read sorted key + rid, write words, keys, offsets), and
+    # the build count before it reads the same 8n.  When both digits of a
+    # two-pass column vary (key-start mode), pass 0 writes one packed word
+    # per row (row offset in its range and high digit: 8n; the range scan
+    # before it zeroes the n/8 bytes of key-start bits), the pass-1 count
+    # reads those words (4n), the key starts write the keys (4K), pass 1
+    # reads the words and writes row ids (8n), and the build count and the
+    # emit each read row ids and bits (4n + n/8; the emit writes 4L + 4K).
+    # Short pass-0 ranges keep the 16-bit exchange (10n per pass).  A phase
+    # (count + scan + kernel) and its main kernel are credited the same
+    # bytes, except the pass-1 count and the build count; the roofline is
+    # taken on the longest single kernel.
     passes = max(1, -(-(card - 1).bit_length() // 8))
     mid16 = passes == 2
     derive = mid16 and card > 256
+    rows_in = 4 * n + n // 8 if derive else 8 * n
     alg = {"histogram": 4 * n, "plan": 0,
-           "build": (4 * n + n // 8 if derive else 8 * n) + 4 * L + 8 * K}
-    alg["emit"] = alg["build"]
+           "emit": rows_in + 4 * L + (4 * K if derive else 8 * K)}
+    alg["build"] = alg["emit"] + rows_in  # the build count reads the same rows first
+    # the packed exchange runs when a pass-0 range (a whole number of
+    # 256 x items-row tiles, SMs x resident CTAs ranges) holds 2^16..2^24 rows
+    tuning = int(lib.wah_get_tuning())
+    items = tuning & 0xFF
+    ranges = torch.cuda.get_device_properties(dev).multi_processor_count * \
+        {8: 4, 12: 3, 16: 2}.get(items, 2)
+    quantum = 256 * max(items, 1)
+    range_rows = max(-(-(-(-n // ranges)) // quantum) * quantum, quantum)
+    packed = derive and range_rows < (1 << 24) and (range_rows >= (1 << 16) or tuning & 0x400)
     for p in range(4):
         if p >= passes:
             a = 0
+        elif packed:
+            a = 8 * n  # pass 0: key in, packed word out; pass 1: packed word in, rid out
         elif derive:
-            a = 8 * n if p == 0 else 8 * n + n // 8
+            a = 10 * n  # pass 0: key in, 16-bit key + rid out; pass 1: both in, rid out
         elif mid16:
             a = 10 * n if p == 0 else 14 * n
         else:
@@ -1249,7 +1265,9 @@ def main():
         alg[f"pass{p}"] = a
         alg[f"scatter{p}"] = a
     if derive:
-        alg["pass1"] += 4 * n  # the count over the packed words
+        alg["pass0"] += n // 8  # the range scan zeroes the key-start bits
+        # the count over the pass-0 output; the key starts write the keys
+        alg["pass1"] += (4 * n if packed else 2 * n) + 4 * K
     # DRAM bytes per row of each kernel (dram__bytes_read.sum +
     # dram__bytes_write.sum, one ncu capture of a 67,108,864-row uniform
     # 16-bit column with the same tile shape); traffic grows with rows.
@@ -1257,16 +1275,17 @@ def main():
     # DRAM bytes per row of each phase (every kernel of it), same capture
     phase_dram_per_row = {"histogram": 4.05, "pass0": 8.86, "pass1": 13.02, "build": 15.45}
     dram_bytes = (sum(phase_dram_per_row.values()) * n
-                  if card == 65536 and derive else None)
+                  if card == 65536 and packed else None)
     per_unit = {"histogram": "4 B/row",
-                "scatter0": ("8 B/row (key in, packed row offset + high digit out)" if derive
+                "scatter0": ("8 B/row (key in, packed row offset + high digit out)" if packed
                              else "10 B/row (key in, 16-bit key + rid out)" if mid16
                              else "12 B/row (key in, key + rid out)"),
-                "scatter1": ("8 B/row + 1 bit (packed word in, rid out, key-start bit)"
-                             if derive else
-                             "14 B/row (16-bit key + rid in, key + rid out)" if mid16
+                "scatter1": ("8 B/row (packed word in, rid out)" if packed
+                             else "10 B/row (16-bit key + rid in, rid out)" if derive
+                             else "14 B/row (16-bit key + rid in, key + rid out)" if mid16
                              else "16 B/row (key + rid in and out)"),
-                "emit": ("4 B/row + 1 bit + 4 B/word + 8 B/key" if derive
+                "emit": ("4 B/row + 1 bit + 4 B/word + 4 B/key (offsets; the key starts "
+                         "write the keys)" if derive
                          else "8 B/row + 4 B/word + 8 B/key")}
     dom = max(KERNELS, key=lambda p: phase_ms[p])
     peak, peak_kind = load_peaks()
@@ -1322,8 +1341,9 @@ def main():
     if cub is not None:
         ours = sum(phase_ms[p] for p in ("histogram", "plan", "pass0", "pass1", "pass2", "pass3"))
         cub["ours_sort_phase_ms"] = ours
-        cub["note"] = ("ours: histogram + digit passes of the index build (16-bit keys between "
-                       "the passes, row ids only out of the last); CUB: SortPairs of the column's "
+        cub["note"] = ("ours: histogram + digit passes of the index build (one packed word per "
+                       "row between the passes where key-start mode packs, else 16-bit keys; row "
+                       "ids and key-start bits out of the last); CUB: SortPairs of the column's "
                        "(value, row id)")
     decode = None if args.no_decode else bench_decode(args, lib, torch, dev, stream, bufs, n, K, L)
     append = (None if args.no_append else
@@ -1425,7 +1445,8 @@ def main():
                          "achieved": ach, "peak": peak, "unit": "GB/s",
                          "frac": ach / peak, "peak_kind": peak_kind,
                          "traffic": (traffic_per_row[dom] * n
-                                     if card == 65536 and dom in traffic_per_row else None),
+                                     if card == 65536 and packed and dom in traffic_per_row
+                                     else None),
                          "traffic_source": "ncu capture at 67,108,864 rows (12-row tiles in "
                                            "both digit passes), scaled by rows"},
             "gpu_launches": launches,
