@@ -91,23 +91,26 @@ constexpr size_t kAlign = 256;
 inline size_t align_up(size_t x) { return (x + kAlign - 1) / kAlign * kAlign; }
 
 struct WsLayout {
-  size_t ctrl, range_hist, range_start, seg0, range_counts, range_first, keyhist, keystart,
-      keys_a, rids_a, keys_b, rids_b, total;
+  size_t ctrl, range_hist, range_counts, zero_end, range_start, seg0, range_first, keyhist,
+      keystart, keys_a, rids_a, keys_b, rids_b, total;
 };
 
 WsLayout ws_layout(uint64_t n) {
   WsLayout l;
   size_t off = 0;
+  // the control block, the histograms and the range counts are contiguous:
+  // one memset clears them before each build
   l.ctrl = off;
   off += align_up(sizeof(WahCtrl));
   l.range_hist = off;  // per-range histograms, then the bin totals of each pass
   off += align_up((size_t)kDigits * (kMaxRanges + kBinTotCopies) * kRadix * sizeof(uint32_t));
+  l.range_counts = off;
+  off += align_up((size_t)kMaxRanges * 4 * sizeof(uint32_t));
+  l.zero_end = off;
   l.range_start = off;
   off += align_up((size_t)kMaxRanges * kRadix * sizeof(uint32_t));
   l.seg0 = off;
   off += align_up((size_t)kMaxRanges * kRadix * sizeof(uint32_t));
-  l.range_counts = off;
-  off += align_up((size_t)kMaxRanges * 4 * sizeof(uint32_t));
   l.range_first = off;
   off += align_up((size_t)kMaxRanges * 2 * sizeof(uint32_t));
   l.keyhist = off;
@@ -150,6 +153,8 @@ void workspace_views(const WsLayout& l, unsigned char* ws, uint64_t n, ColumnVie
   ra->counts = reinterpret_cast<uint32_t*>(ws + l.range_counts);
   ra->first = reinterpret_cast<uint32_t*>(ws + l.range_first);
   ra->max_ranges = kMaxRanges;
+  ra->zero = ws + l.ctrl;
+  ra->zero_bytes = l.zero_end - l.ctrl;
 }
 
 }  // namespace
@@ -202,9 +207,7 @@ static int build_impl(const uint32_t* d_values, uint64_t n, uint32_t bound, uint
   if (!d_counts || !aligned16(d_counts)) return WAH_EINVAL;
   if (n >= WAH_MAX_ROWS) return WAH_ERANGE;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  cudaError_t e = cudaMemsetAsync(d_counts, 0, sizeof(wah_counts), s);
-  if (e != cudaSuccess) return cuda_status(e);
-  if (n == 0) return WAH_OK;
+  if (n == 0) return cuda_status(cudaMemsetAsync(d_counts, 0, sizeof(wah_counts), s));
   if (!d_values || !d_keys || !d_offsets || !d_index || !d_workspace) return WAH_EINVAL;
   if (!aligned16(d_values) || !aligned16(d_workspace)) return WAH_EINVAL;
   const WsLayout l = ws_layout(n);
@@ -217,15 +220,14 @@ static int build_impl(const uint32_t* d_values, uint64_t n, uint32_t bound, uint
   c.offsets = d_offsets;
   c.index = d_index;
   wah_output_caps(n, bound, &c.keys_cap, &c.index_cap);
-  c.counts = d_counts;
+  c.counts = d_counts;  // zeroed by the histogram kernel, the build's first
   c.status = &d_counts->status;
   c.passes = passes_for_bound(bound);
   c.derive_ok = 1;  // an index build: the sorted keys themselves are never read back
   const LaunchOpts o = launch_opts(c.passes, events, tuning);
   if (o.sm_count <= 0) return WAH_ENODEV;
-  e = cudaMemsetAsync(c.ctrl, 0, sizeof(WahCtrl), s);
-  if (e != cudaSuccess) return cuda_status(e);
-  e = launch_sort_one(c, ra, o, s, &g_last_launches);
+  // the control block is cleared with the histograms (launch_sort_one)
+  cudaError_t e = launch_sort_one(c, ra, o, s, &g_last_launches);
   if (e != cudaSuccess) return cuda_status(e);
   return cuda_status(launch_build_one(c, ra, o, s, &g_last_launches));
 }
@@ -298,9 +300,8 @@ int wah_sort_rids_by_value(const uint32_t* d_values, uint64_t n, uint32_t bound,
   c.passes = passes_for_bound(bound);
   const LaunchOpts o = launch_opts(c.passes, nullptr);
   if (o.sm_count <= 0) return WAH_ENODEV;
-  cudaError_t e = cudaMemsetAsync(c.ctrl, 0, sizeof(WahCtrl), s);
-  if (e != cudaSuccess) return cuda_status(e);
-  e = launch_sort_one(c, ra, o, s, &g_last_launches);
+  // the control block is cleared with the histograms (launch_sort_one)
+  cudaError_t e = launch_sort_one(c, ra, o, s, &g_last_launches);
   if (e != cudaSuccess) return cuda_status(e);
   // Deliver the device-chosen final home into the caller's buffers.
   return cuda_status(launch_sort_deliver(c, d_sorted_values, d_rids, s, &g_last_launches));
@@ -337,7 +338,8 @@ int wah_build_sorted(const uint32_t* d_sorted_values, const uint32_t* d_rids, ui
   c.passes = kDigits;
   const LaunchOpts o = launch_opts(kDigits, nullptr);
   if (o.sm_count <= 0) return WAH_ENODEV;
-  e = cudaMemsetAsync(c.ctrl, 0, sizeof(WahCtrl), s);
+  // no sort: the control block and the range counts are cleared here
+  e = cudaMemsetAsync(ra.zero, 0, ra.zero_bytes, s);
   if (e != cudaSuccess) return cuda_status(e);
   return cuda_status(launch_build_one(c, ra, o, s, &g_last_launches));
 }

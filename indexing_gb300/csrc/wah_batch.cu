@@ -166,6 +166,8 @@ cudaError_t enqueue_batch(const BatchLayout& L, unsigned char* dev, cudaStream_t
   ra.counts = reinterpret_cast<uint32_t*>(dev + L.o_counts);
   ra.first = reinterpret_cast<uint32_t*>(dev + L.o_rfirst);
   ra.max_ranges = std::max<uint32_t>(L.nranges, 1);
+  ra.zero = ra.hist;
+  ra.zero_bytes = (size_t)kDigits * ra.max_ranges * kRadix * sizeof(uint32_t);
   e = launch_sort_many(g, L.ncols, L.nranges, ra, o, s, launches);
   if (e != cudaSuccess) return e;
   return launch_build_many(g, L.ncols, L.nranges, ra, o, s, launches);

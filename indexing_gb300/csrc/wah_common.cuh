@@ -397,6 +397,12 @@ struct RangeArrays {
   uint32_t* counts;  // [max_ranges][4] words, keys, segments per range
   uint32_t* first;   // [max_ranges][2] first word and key per range
   uint32_t max_ranges;
+  // cleared by one memset before the histogram: for one column the control
+  // block, the histograms, the bin totals and the range counts (contiguous
+  // in the workspace); for batches the histograms (their range counts are
+  // cleared before the build count)
+  void* zero;
+  size_t zero_bytes;
 };
 
 // Tuning and instrumentation of one launch sequence.

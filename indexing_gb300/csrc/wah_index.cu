@@ -599,8 +599,10 @@ cudaError_t launch_build_t(const G& g, uint32_t ncols, uint32_t ranges, const Ra
   cudaError_t err = cudaFuncSetAttribute(k_build_emit<G>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (err != cudaSuccess) return err;
-  err = cudaMemsetAsync(ra.counts, 0, (size_t)ra.max_ranges * 4 * sizeof(uint32_t), s);
-  if (err != cudaSuccess) return err;
+  if constexpr (!std::is_same<G, OneColumn>::value) {  // one column: cleared before the sort
+    err = cudaMemsetAsync(ra.counts, 0, (size_t)ra.max_ranges * 4 * sizeof(uint32_t), s);
+    if (err != cudaSuccess) return err;
+  }
   record_phase(o.events, kPhaseBuild, false, s);
   k_build_count<G><<<ranges * kCountCtasPerRange, kHistThreads, 0, s>>>(g, ra.counts);
   if constexpr (!std::is_same<G, OneColumn>::value) {  // one column: inside the emit

@@ -181,29 +181,37 @@ __device__ __forceinline__ void count_packed_keys(const uint32_t* __restrict__ w
   uint32_t* h1 = s_h[warp][0];  // digit-1 counts of the range
   uint32_t* hw = s_full[warp];  // digit-1 counts for the warp's current low digit
   uint32_t cur = kRadix;        // the low digit hw counts (none yet)
+  uint32_t cur_lo = 0, cur_hi = 0;  // its positions [cur_lo, cur_hi)
   const uint4* wv = reinterpret_cast<const uint4*>(words + lo);
   const uint64_t chunks = (hi - lo) / 128;  // 32 lanes x 4 words
   auto add_chunk = [&](const uint4& q, uint64_t c) {
     const uint32_t c0 = (uint32_t)(lo + c * 128);
-    const uint32_t d0 = bin_of(binoff, c0);
-    if (c0 + 127 < binoff[d0 + 1]) {
+    // a warp's chunks ascend, so most lie in the bin of the chunk before:
+    // the bin is looked up only when a chunk leaves it
+    if (!(c0 >= cur_lo && c0 + 127 < cur_hi)) {
+      const uint32_t d0 = bin_of(binoff, c0);
+      const uint32_t d_hi = binoff[d0 + 1];
+      if (c0 + 127 >= d_hi) {  // the chunk spans low digits: row by row
+        const uint32_t w4[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const uint32_t d1 = w4[i] & 0xFFu;
+          atomicAdd(&h1[d1], 1u);
+          atomicAdd(&keyhist[(d1 << 8) | bin_of(binoff, c0 + lane * 4 + i)], 1u);
+        }
+        return;
+      }
       if (d0 != cur) {
         if (cur < kRadix) flush_keyhist(hw, h1, cur, lane, keyhist);
         cur = d0;
       }
-      atomicAdd(&hw[q.x & 0xFFu], 1u);
-      atomicAdd(&hw[q.y & 0xFFu], 1u);
-      atomicAdd(&hw[q.z & 0xFFu], 1u);
-      atomicAdd(&hw[q.w & 0xFFu], 1u);
-    } else {
-      const uint32_t w4[4] = {q.x, q.y, q.z, q.w};
-#pragma unroll
-      for (int i = 0; i < 4; ++i) {
-        const uint32_t d1 = w4[i] & 0xFFu;
-        atomicAdd(&h1[d1], 1u);
-        atomicAdd(&keyhist[(d1 << 8) | bin_of(binoff, c0 + lane * 4 + i)], 1u);
-      }
+      cur_lo = binoff[d0];
+      cur_hi = d_hi;
     }
+    atomicAdd(&hw[q.x & 0xFFu], 1u);
+    atomicAdd(&hw[q.y & 0xFFu], 1u);
+    atomicAdd(&hw[q.z & 0xFFu], 1u);
+    atomicAdd(&hw[q.w & 0xFFu], 1u);
   };
   uint64_t c = warp;
   for (; c + (kHistUnroll - 1) * nwarps < chunks; c += kHistUnroll * nwarps) {
@@ -317,6 +325,12 @@ __global__ void __launch_bounds__(kHistThreads)
   const uint32_t r = blockIdx.x / parts;
   const RangeView rv = g.range(r);
   const ColumnView c = g.col(rv.col);
+  if constexpr (std::is_same<G, OneColumn>::value) {
+    // an index build's result counters start at zero here: no kernel of the
+    // build before this one, and none in it sets a status
+    if (blockIdx.x == 0 && threadIdx.x == 0 && c.counts)
+      *reinterpret_cast<uint4*>(c.counts) = make_uint4(0, 0, 0, 0);
+  }
   uint64_t lo, hi;
   sub_range(rv, blockIdx.x % parts, parts, &lo, &hi);
   const uint2 acc = histogram_range<1>(c.input, lo, hi, 0, s_h);
@@ -1247,11 +1261,9 @@ cudaError_t launch_sort_t(const G& g0, uint32_t ranges0, const SortVariant<G>& v
     if (g1.count_parts) parts1 = g1.count_parts;
   }
   const unsigned count_grid = ranges0 * parts0;
-  // the per-range histograms (and, for one column, the bin totals after them)
-  cudaError_t err = cudaMemsetAsync(
-      ra.hist, 0,
-      ((size_t)kDigits * ra.max_ranges + (ra.bintot ? kBinTotCopies * kDigits : 0)) * kRadix * 4,
-      s);
+  // the per-range histograms (for one column with the control block before
+  // them and the bin totals and emit state after them)
+  cudaError_t err = cudaMemsetAsync(ra.zero, 0, ra.zero_bytes, s);
   if (err != cudaSuccess) return err;
   record_phase(o.events, kPhaseHist, false, s);
   k_digit_histogram<G><<<count_grid, kHistThreads, 0, s>>>(g0, ra.hist);
