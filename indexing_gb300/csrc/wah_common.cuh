@@ -180,6 +180,18 @@ __device__ __forceinline__ void set_status(uint32_t* status, uint32_t code) {
   if (status) atomicCAS(status, 0u, code);
 }
 
+// Programmatic dependent launch: the build's kernels are launched with
+// launch_pdl, and every one of them calls this first.  It waits until the
+// kernel before it on the stream has finished and its writes are visible,
+// then lets the kernel after it be scheduled (its CTAs take free SM slots
+// and wait in this same call, instead of waiting for a launch after this
+// grid drains).  Both are no-ops for a normal launch.  The wait comes first,
+// so at most two grids of a stream are resident at a time.
+__device__ __forceinline__ void griddep_wait() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 // Exclusive scan of one u32 per thread across a block of up to 256 threads
 // with one barrier: warp scans, then every thread adds up the totals of the
 // warps before its own.  The caller keeps a barrier between its reads of
@@ -287,6 +299,29 @@ constexpr int kPhases = 12;
 inline void record_phase(cudaEvent_t* ev, int phase, bool end, cudaStream_t s) {
   if (ev) cudaEventRecord(ev[2 * phase + (end ? 1 : 0)], s);
 }
+
+#if defined(__CUDACC__)
+// Launches a kernel of the build with programmatic stream serialization: it
+// may be scheduled while the kernel before it on the stream drains (and, in
+// a captured graph, through a programmatic edge), and waits for that kernel
+// with griddep_wait before touching memory.  Saves a launch gap per kernel
+// boundary, which is what small columns are made of.
+template <typename... KArgs, typename... Args>
+cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                       cudaStream_t s, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+#endif
 
 // ---------------------------------------------------------------------------
 // Columns and ranges as the kernels see them.

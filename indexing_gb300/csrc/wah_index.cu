@@ -83,6 +83,7 @@ __device__ __forceinline__ void count_row(uint32_t v, uint32_t c, uint32_t pv, u
 template <class G>
 __global__ void __launch_bounds__(kHistThreads)
     k_build_count(G g, uint32_t* __restrict__ range_counts /* [ranges][4] */) {
+  griddep_wait();
   const uint32_t c = blockIdx.x / kCountCtasPerRange, q = blockIdx.x % kCountCtasPerRange;
   const RangeView rv = g.range(c);
   const ColumnView col = g.col(rv.col);
@@ -213,6 +214,7 @@ template <class G>
 __global__ void __launch_bounds__(kBuildScanThreads)
     k_build_scan(G g, const uint32_t* __restrict__ range_counts,
                  uint32_t* __restrict__ range_first /* [ranges][2] */) {
+  griddep_wait();
   __shared__ uint64_t s_warp[kBuildScanThreads / 32 + 1];
   const ColumnView col = g.col(blockIdx.x);
   const uint32_t r0 = g.first_range(blockIdx.x), r1 = g.end_range(blockIdx.x);
@@ -577,6 +579,7 @@ __device__ __forceinline__ void build_emit(const G& g, const uint32_t* __restric
 template <class G>
 __global__ void __launch_bounds__(kBuildThreads, 4)
     k_build_emit(G g, const uint32_t* __restrict__ range_first) {
+  griddep_wait();
   extern __shared__ __align__(128) unsigned char smem_raw[];
   EmitSmem& sm = *reinterpret_cast<EmitSmem*>(smem_raw);
   if constexpr (std::is_same<G, OneColumn>::value) {
@@ -604,18 +607,23 @@ cudaError_t launch_build_t(const G& g, uint32_t ncols, uint32_t ranges, const Ra
     if (err != cudaSuccess) return err;
   }
   record_phase(o.events, kPhaseBuild, false, s);
-  k_build_count<G><<<ranges * kCountCtasPerRange, kHistThreads, 0, s>>>(g, ra.counts);
+  err = launch_pdl(k_build_count<G>, ranges * kCountCtasPerRange, kHistThreads, 0, s, g,
+                   ra.counts);
+  if (err != cudaSuccess) return err;
   if constexpr (!std::is_same<G, OneColumn>::value) {  // one column: inside the emit
-    k_build_scan<G><<<ncols, kBuildScanThreads, 0, s>>>(g, ra.counts, ra.first);
+    err = launch_pdl(k_build_scan<G>, ncols, kBuildScanThreads, 0, s, g,
+                     (const uint32_t*)ra.counts, ra.first);
+    if (err != cudaSuccess) return err;
     ++*launches;
   }
   record_phase(o.events, kPhaseEmit, false, s);
-  k_build_emit<G><<<ranges, kBuildThreads, smem, s>>>(
-      g, std::is_same<G, OneColumn>::value ? ra.counts : ra.first);
+  err = launch_pdl(k_build_emit<G>, ranges, kBuildThreads, smem, s, g,
+                   (const uint32_t*)(std::is_same<G, OneColumn>::value ? ra.counts : ra.first));
+  if (err != cudaSuccess) return err;
   record_phase(o.events, kPhaseEmit, true, s);
   record_phase(o.events, kPhaseBuild, true, s);
   *launches += 2;
-  return cudaGetLastError();
+  return cudaSuccess;
 }
 
 cudaError_t launch_build_one(const ColumnView& c, const RangeArrays& ra, const LaunchOpts& o,

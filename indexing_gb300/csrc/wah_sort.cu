@@ -318,6 +318,7 @@ __device__ __forceinline__ void add_bin_total(const G& g, int pass, uint32_t bin
 template <class G>
 __global__ void __launch_bounds__(kHistThreads)
     k_digit_histogram(G g, uint32_t* __restrict__ range_hist0) {
+  griddep_wait();
   __shared__ uint32_t s_h[kHistWarps][1][kRadix];
   for (int i = threadIdx.x; i < kHistWarps * kRadix; i += kHistThreads) (&s_h[0][0][0])[i] = 0;
   __syncthreads();
@@ -354,6 +355,7 @@ __global__ void __launch_bounds__(kHistThreads)
 template <class G>
 __global__ void __launch_bounds__(kHistThreads)
     k_range_count(G g, int pass, uint32_t* __restrict__ range_hist) {
+  griddep_wait();
   const uint32_t parts = count_parts(g);
   const uint32_t r = blockIdx.x / parts;
   const RangeView rv = g.range(r);
@@ -446,6 +448,7 @@ __device__ __forceinline__ int plan_column(const ColumnView& c, bool write) {
 
 template <class G>
 __global__ void __launch_bounds__(kRadix) k_sort_plan(G g) {
+  griddep_wait();
   if (threadIdx.x == 0) plan_column(g.col(blockIdx.x), true);
 }
 
@@ -502,6 +505,7 @@ template <class G>
 __global__ void __launch_bounds__(kRangeScanThreads)
     k_range_scan(G g, int pass, const uint32_t* __restrict__ range_hist,
                  uint32_t* __restrict__ range_start) {
+  griddep_wait();
   __shared__ uint32_t s_warp[kRangeScanThreads / 32 + 1];
   __shared__ uint32_t s_part[kRangeScanParts][kRadix];
   const ColumnView col = g.col(blockIdx.x);
@@ -560,6 +564,7 @@ static_assert(kKeyStartThreads == kRangeScanOneThreads, "key-start CTAs share th
 __global__ void __launch_bounds__(kRangeScanOneThreads)
     k_range_scan_one(OneColumn g, int pass, const uint32_t* __restrict__ range_hist,
                      uint32_t* __restrict__ range_start) {
+  griddep_wait();
   __shared__ uint32_t s_warp[kRangeScanOneThreads / 32 + 1];
   __shared__ uint64_t s_warp64[kRangeScanOneThreads / 32 + 1];
   if (blockIdx.x >= kRadix) {  // digit pass 1: the key starts
@@ -1068,6 +1073,7 @@ __device__ __forceinline__ void scatter_pack1(const OneColumn& g,
 template <int ITEMS, int PEERS, class G>
 __global__ void __launch_bounds__(kSortThreads, ITEMS <= 12 ? 3 : 2)
     k_radix_scatter(G g, int pass, const uint32_t* __restrict__ range_start) {
+  griddep_wait();
   constexpr uint32_t TILE = kSortThreads * ITEMS;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   ScatterSmem<ITEMS>& sm = *reinterpret_cast<ScatterSmem<ITEMS>*>(smem_raw);
@@ -1262,21 +1268,21 @@ cudaError_t launch_sort_t(const G& g0, uint32_t ranges0, const SortVariant<G>& v
   }
   const unsigned count_grid = ranges0 * parts0;
   // the per-range histograms (for one column with the control block before
-  // them and the bin totals and emit state after them)
+  // them and the bin totals and range counts after them)
   cudaError_t err = cudaMemsetAsync(ra.zero, 0, ra.zero_bytes, s);
   if (err != cudaSuccess) return err;
   record_phase(o.events, kPhaseHist, false, s);
-  k_digit_histogram<G><<<count_grid, kHistThreads, 0, s>>>(g0, ra.hist);
+  err = launch_pdl(k_digit_histogram<G>, count_grid, kHistThreads, 0, s, g0, ra.hist);
+  if (err != cudaSuccess) return err;
   record_phase(o.events, kPhaseHist, true, s);
   ++*launches;
   record_phase(o.events, kPhasePlan, false, s);
   if constexpr (!std::is_same<G, OneColumn>::value) {  // one column: in the pass-0 range scan
-    k_sort_plan<G><<<ncols, kRadix, 0, s>>>(g0);
+    err = launch_pdl(k_sort_plan<G>, ncols, kRadix, 0, s, g0);
+    if (err != cudaSuccess) return err;
     ++*launches;
   }
   record_phase(o.events, kPhasePlan, true, s);
-  err = cudaGetLastError();
-  if (err != cudaSuccess) return err;
   for (int p = 0; p < kDigits; ++p) {
     if (p >= o.max_passes) {  // not launched: empty spans keep every event valid
       record_phase(o.events, kPhasePass0 + p, false, s);
@@ -1291,17 +1297,22 @@ cudaError_t launch_sort_t(const G& g0, uint32_t ranges0, const SortVariant<G>& v
     const SortVariant<G>& v = p == 0 ? v0 : v1;
     record_phase(o.events, kPhasePass0 + p, false, s);
     if (p > 0) {
-      k_range_count<G><<<ranges * (p == 0 ? parts0 : parts1), kHistThreads, 0, s>>>(gp, p, rh);
+      err = launch_pdl(k_range_count<G>, ranges * (p == 0 ? parts0 : parts1), kHistThreads, 0, s,
+                       gp, p, rh);
+      if (err != cudaSuccess) return err;
       ++*launches;
     }
     if constexpr (std::is_same<G, OneColumn>::value)  // + the key starts for digit pass 1
-      k_range_scan_one<<<kRadix + (p == 1 && gp.c.derive_ok ? kKeyStartCtas : 0),
-                         kRangeScanOneThreads, 0, s>>>(gp, p, rh, ra.start);
+      err = launch_pdl(k_range_scan_one, kRadix + (p == 1 && gp.c.derive_ok ? kKeyStartCtas : 0),
+                       kRangeScanOneThreads, 0, s, gp, p, (const uint32_t*)rh, ra.start);
     else
-      k_range_scan<G><<<ncols, kRangeScanThreads, 0, s>>>(gp, p, rh, ra.start);
+      err = launch_pdl(k_range_scan<G>, ncols, kRangeScanThreads, 0, s, gp, p,
+                       (const uint32_t*)rh, ra.start);
+    if (err != cudaSuccess) return err;
     ++*launches;
     record_phase(o.events, kPhaseScatter0 + p, false, s);
-    v.fn<<<ranges, kSortThreads, v.smem, s>>>(gp, p, ra.start);
+    err = launch_pdl(v.fn, ranges, kSortThreads, v.smem, s, gp, p, (const uint32_t*)ra.start);
+    if (err != cudaSuccess) return err;
     ++*launches;
     record_phase(o.events, kPhaseScatter0 + p, true, s);
     record_phase(o.events, kPhasePass0 + p, true, s);
