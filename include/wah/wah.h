@@ -86,7 +86,9 @@ size_t wah_workspace_bytes(uint64_t n, uint32_t bound);
  * sort runs ceil(bits(bound)/8) digit passes; values above it are reported
  * as WAH_ERANGE in d_counts->status.
  * d_keys/d_offsets: capacity from wah_output_caps; d_index: 2n words.
- * d_counts: device wah_counts, written at the end of the build.
+ * d_counts: device wah_counts (16-byte aligned), cleared by the build's
+ * first kernel and written at its end; a call that returns an error code
+ * before enqueueing anything leaves it untouched.
  * The call enqueues work and returns; nothing is synchronised.
  * n == 0 writes K = L = 0 (the reference is undefined there).
  */

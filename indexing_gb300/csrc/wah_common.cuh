@@ -180,16 +180,15 @@ __device__ __forceinline__ void set_status(uint32_t* status, uint32_t code) {
   if (status) atomicCAS(status, 0u, code);
 }
 
-// Programmatic dependent launch: the build's kernels are launched with
-// launch_pdl, and every one of them calls this first.  It waits until the
-// kernel before it on the stream has finished and its writes are visible,
-// then lets the kernel after it be scheduled (its CTAs take free SM slots
-// and wait in this same call, instead of waiting for a launch after this
-// grid drains).  Both are no-ops for a normal launch.  The wait comes first,
-// so at most two grids of a stream are resident at a time.
+// Programmatic dependent launch: a one-column build's kernels are launched
+// with launch_kernel(programmatic = true), so each is launched as the one
+// before it on the stream finishes rather than after it has drained, and
+// every kernel of a build calls this first: it waits until that kernel has
+// finished and its writes are visible (a no-op for a normal launch).  No
+// kernel triggers its dependents early: CTAs parked in this wait would hold
+// SM slots, which cost the many-stream serving mix its tail latency.
 __device__ __forceinline__ void griddep_wait() {
   asm volatile("griddepcontrol.wait;" ::: "memory");
-  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
 
 // Exclusive scan of one u32 per thread across a block of up to 256 threads
@@ -301,14 +300,15 @@ inline void record_phase(cudaEvent_t* ev, int phase, bool end, cudaStream_t s) {
 }
 
 #if defined(__CUDACC__)
-// Launches a kernel of the build with programmatic stream serialization: it
-// may be scheduled while the kernel before it on the stream drains (and, in
-// a captured graph, through a programmatic edge), and waits for that kernel
-// with griddep_wait before touching memory.  Saves a launch gap per kernel
-// boundary, which is what small columns are made of.
+// Launches a kernel of a build; programmatic: with programmatic stream
+// serialization, so it is launched while the kernel before it on the stream
+// finishes (in a captured graph, through a programmatic edge) and waits for
+// it in griddep_wait before touching memory.  That saves a launch gap per
+// kernel boundary, which is what small columns are made of; one-column
+// builds use it, batches (the serving mix, several streams) do not.
 template <typename... KArgs, typename... Args>
-cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem,
-                       cudaStream_t s, Args... args) {
+cudaError_t launch_kernel(bool programmatic, void (*kernel)(KArgs...), dim3 grid, dim3 block,
+                          size_t smem, cudaStream_t s, Args... args) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = grid;
   cfg.blockDim = block;
@@ -318,7 +318,7 @@ cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t s
   attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
   attr[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = attr;
-  cfg.numAttrs = 1;
+  cfg.numAttrs = programmatic ? 1 : 0;
   return cudaLaunchKernelEx(&cfg, kernel, args...);
 }
 #endif

@@ -598,6 +598,7 @@ __global__ void __launch_bounds__(kBuildThreads, 4)
 template <class G>
 cudaError_t launch_build_t(const G& g, uint32_t ncols, uint32_t ranges, const RangeArrays& ra,
                            const LaunchOpts& o, cudaStream_t s, uint32_t* launches) {
+  constexpr bool kPdl = std::is_same<G, OneColumn>::value;  // programmatic launches
   const size_t smem = sizeof(EmitSmem);
   cudaError_t err = cudaFuncSetAttribute(k_build_emit<G>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -607,17 +608,17 @@ cudaError_t launch_build_t(const G& g, uint32_t ncols, uint32_t ranges, const Ra
     if (err != cudaSuccess) return err;
   }
   record_phase(o.events, kPhaseBuild, false, s);
-  err = launch_pdl(k_build_count<G>, ranges * kCountCtasPerRange, kHistThreads, 0, s, g,
+  err = launch_kernel(kPdl,k_build_count<G>, ranges * kCountCtasPerRange, kHistThreads, 0, s, g,
                    ra.counts);
   if (err != cudaSuccess) return err;
   if constexpr (!std::is_same<G, OneColumn>::value) {  // one column: inside the emit
-    err = launch_pdl(k_build_scan<G>, ncols, kBuildScanThreads, 0, s, g,
+    err = launch_kernel(kPdl,k_build_scan<G>, ncols, kBuildScanThreads, 0, s, g,
                      (const uint32_t*)ra.counts, ra.first);
     if (err != cudaSuccess) return err;
     ++*launches;
   }
   record_phase(o.events, kPhaseEmit, false, s);
-  err = launch_pdl(k_build_emit<G>, ranges, kBuildThreads, smem, s, g,
+  err = launch_kernel(kPdl,k_build_emit<G>, ranges, kBuildThreads, smem, s, g,
                    (const uint32_t*)(std::is_same<G, OneColumn>::value ? ra.counts : ra.first));
   if (err != cudaSuccess) return err;
   record_phase(o.events, kPhaseEmit, true, s);

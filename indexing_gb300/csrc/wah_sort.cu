@@ -1261,6 +1261,7 @@ cudaError_t launch_sort_t(const G& g0, uint32_t ranges0, const SortVariant<G>& v
                           uint32_t ranges1, const SortVariant<G>& v1, uint32_t ncols,
                           const RangeArrays& ra, const LaunchOpts& o, cudaStream_t s,
                           uint32_t* launches) {
+  constexpr bool kPdl = std::is_same<G, OneColumn>::value;  // programmatic launches
   uint32_t parts0 = kCountCtasPerRange, parts1 = kCountCtasPerRange;
   if constexpr (std::is_same<G, OneColumn>::value) {
     if (g0.count_parts) parts0 = g0.count_parts;
@@ -1272,13 +1273,13 @@ cudaError_t launch_sort_t(const G& g0, uint32_t ranges0, const SortVariant<G>& v
   cudaError_t err = cudaMemsetAsync(ra.zero, 0, ra.zero_bytes, s);
   if (err != cudaSuccess) return err;
   record_phase(o.events, kPhaseHist, false, s);
-  err = launch_pdl(k_digit_histogram<G>, count_grid, kHistThreads, 0, s, g0, ra.hist);
+  err = launch_kernel(kPdl,k_digit_histogram<G>, count_grid, kHistThreads, 0, s, g0, ra.hist);
   if (err != cudaSuccess) return err;
   record_phase(o.events, kPhaseHist, true, s);
   ++*launches;
   record_phase(o.events, kPhasePlan, false, s);
   if constexpr (!std::is_same<G, OneColumn>::value) {  // one column: in the pass-0 range scan
-    err = launch_pdl(k_sort_plan<G>, ncols, kRadix, 0, s, g0);
+    err = launch_kernel(kPdl,k_sort_plan<G>, ncols, kRadix, 0, s, g0);
     if (err != cudaSuccess) return err;
     ++*launches;
   }
@@ -1297,21 +1298,21 @@ cudaError_t launch_sort_t(const G& g0, uint32_t ranges0, const SortVariant<G>& v
     const SortVariant<G>& v = p == 0 ? v0 : v1;
     record_phase(o.events, kPhasePass0 + p, false, s);
     if (p > 0) {
-      err = launch_pdl(k_range_count<G>, ranges * (p == 0 ? parts0 : parts1), kHistThreads, 0, s,
+      err = launch_kernel(kPdl,k_range_count<G>, ranges * (p == 0 ? parts0 : parts1), kHistThreads, 0, s,
                        gp, p, rh);
       if (err != cudaSuccess) return err;
       ++*launches;
     }
     if constexpr (std::is_same<G, OneColumn>::value)  // + the key starts for digit pass 1
-      err = launch_pdl(k_range_scan_one, kRadix + (p == 1 && gp.c.derive_ok ? kKeyStartCtas : 0),
+      err = launch_kernel(kPdl,k_range_scan_one, kRadix + (p == 1 && gp.c.derive_ok ? kKeyStartCtas : 0),
                        kRangeScanOneThreads, 0, s, gp, p, (const uint32_t*)rh, ra.start);
     else
-      err = launch_pdl(k_range_scan<G>, ncols, kRangeScanThreads, 0, s, gp, p,
+      err = launch_kernel(kPdl,k_range_scan<G>, ncols, kRangeScanThreads, 0, s, gp, p,
                        (const uint32_t*)rh, ra.start);
     if (err != cudaSuccess) return err;
     ++*launches;
     record_phase(o.events, kPhaseScatter0 + p, false, s);
-    err = launch_pdl(v.fn, ranges, kSortThreads, v.smem, s, gp, p, (const uint32_t*)ra.start);
+    err = launch_kernel(kPdl,v.fn, ranges, kSortThreads, v.smem, s, gp, p, (const uint32_t*)ra.start);
     if (err != cudaSuccess) return err;
     ++*launches;
     record_phase(o.events, kPhaseScatter0 + p, true, s);
