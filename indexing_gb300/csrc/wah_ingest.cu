@@ -19,8 +19,9 @@
 // range (16 bytes per thread per step, whitespace found with SIMD byte
 // compares), k_parse_scan turns the counts into each range's first token
 // number, and k_parse_emit re-reads the range step by step through shared
-// memory, parses every token that starts in it and writes value i to
-// values[i].  A token of up to 16 characters is converted eight digits at a
+// memory (32 bytes per thread per step: half the per-step scan and barrier
+// work per token of 16), parses every token that starts in it and writes
+// value i to values[i].  A token of up to 16 characters is converted eight digits at a
 // time in 64-bit registers (SWAR); longer ones (leading zeros) character by
 // character.  Invalid tokens lower a device-wide "first invalid token" with
 // atomicMin.  The largest value is reduced while parsing; only when an
@@ -31,7 +32,8 @@ namespace wah {
 namespace {
 
 constexpr int kPThreads = 256;
-constexpr uint32_t kPStep = kPThreads * 16;  // bytes per CTA step
+constexpr uint32_t kPStep = kPThreads * 16;   // bytes per CTA step of the count
+constexpr uint32_t kPEStep = kPThreads * 32;  // bytes per CTA step of the emit
 constexpr uint32_t kMaxParseRanges = 4096;
 constexpr uint64_t kNoInvalid = ~0ull;
 
@@ -82,7 +84,7 @@ __device__ __forceinline__ bool is_ws(uint32_t c) { return c == 0x20u || (c >= 9
 struct ParseIn {
   const unsigned char* text;
   uint64_t bytes;
-  uint64_t range_bytes;  // multiple of kPStep
+  uint64_t range_bytes;  // multiple of kPEStep (and so of kPStep)
   uint32_t ranges;
 };
 
@@ -152,10 +154,11 @@ __global__ void __launch_bounds__(kPScanThreads) k_parse_scan(ParseRange* rng, u
   }
 }
 
-// Bytes a CTA step keeps in shared memory: its own 4096 and the 64 after
-// them, so tokens that start in the step and end shortly after it are read
-// from shared memory too; longer ones continue from global memory.
-constexpr uint32_t kPWindow = kPStep + 64;
+// Bytes an emit step keeps in shared memory: its own 8192 (32 per thread)
+// and the 64 after them, so tokens that start in the step and end shortly
+// after it are read from shared memory too; longer ones continue from
+// global memory.
+constexpr uint32_t kPWindow = kPEStep + 64;
 
 // Parses the token starting at byte p (a token start) of the step at s,
 // character by character.  Returns false if the token is not a 32-bit
@@ -217,44 +220,48 @@ __global__ void __launch_bounds__(kPThreads) k_parse_emit(ParseIn in, const Pars
   const uint32_t lane = threadIdx.x & 31;
   uint64_t carry = rng[blockIdx.x].base;
   uint32_t vmax = 0;
-  for (uint64_t s = lo; s < hi; s += kPStep) {
-    const uint64_t p = s + threadIdx.x * 16ull;
-    // bytes past the range are loaded too (whitespace past the text's end)
-    const uint4 q = load16(in, p);
-    reinterpret_cast<uint4*>(s_text)[threadIdx.x] = q;
+  for (uint64_t s = lo; s < hi; s += kPEStep) {
+    // this thread's 32 bytes (two 16-byte loads); bytes past the range are
+    // loaded too (whitespace past the text's end)
+    const uint64_t p = s + threadIdx.x * 32ull;
+    const uint4 q0 = load16(in, p), q1 = load16(in, p + 16);
+    reinterpret_cast<uint4*>(s_text)[2 * threadIdx.x] = q0;
+    reinterpret_cast<uint4*>(s_text)[2 * threadIdx.x + 1] = q1;
     if (threadIdx.x < 4)
-      reinterpret_cast<uint4*>(s_text + kPStep)[threadIdx.x] =
-          load16(in, s + kPStep + 16ull * threadIdx.x);
-    const uint32_t nw = nonws_mask16(q);
-    // the next 16 bytes' mask: the next lane's, or (last lane) computed here
+      reinterpret_cast<uint4*>(s_text + kPEStep)[threadIdx.x] =
+          load16(in, s + kPEStep + 16ull * threadIdx.x);
+    const uint32_t nw = nonws_mask16(q0) | (nonws_mask16(q1) << 16);
+    // the next 32 bytes' mask: the next lane's, or (last lane) computed here
     uint32_t nw_next = __shfl_down_sync(0xffffffffu, nw, 1);
-    const uint32_t prev_last = __shfl_up_sync(0xffffffffu, nw >> 15, 1);
+    const uint32_t prev_last = __shfl_up_sync(0xffffffffu, nw >> 31, 1);
     __syncthreads();
-    if (lane == 31)
-      nw_next = nonws_mask16(reinterpret_cast<const uint4*>(s_text)[threadIdx.x + 1]);
+    if (lane == 31) {
+      const uint4* nx = reinterpret_cast<const uint4*>(s_text) + 2 * (threadIdx.x + 1);
+      nw_next = nonws_mask16(nx[0]) | (nonws_mask16(nx[1]) << 16);
+    }
     uint32_t st = 0;
     if (p < hi) {
       uint32_t prev_nonws;
       if (lane > 0)
         prev_nonws = prev_last & 1u;
       else if (threadIdx.x > 0)
-        prev_nonws = !is_ws(s_text[threadIdx.x * 16 - 1]);
+        prev_nonws = !is_ws(s_text[threadIdx.x * 32 - 1]);
       else
         prev_nonws = p > 0 && !is_ws(in.text[p - 1]);
-      st = nw & ~((nw << 1) | prev_nonws) & 0xFFFFu;
+      st = nw & ~((nw << 1) | prev_nonws);
     }
     uint32_t tot;
     const uint32_t ex = block_exclusive_scan<kPThreads>(__popc(st), &tot, s_w);
     uint64_t idx = carry + ex;
-    const uint32_t nw32 = nw | (nw_next << 16);
+    const uint64_t nw64 = (uint64_t)nw | ((uint64_t)nw_next << 32);
     uint32_t m = st;
     while (m) {
       const uint32_t b = __ffs(m) - 1;
       m &= m - 1;
-      // token length from the 32-byte non-whitespace mask, if it ends there
-      const uint32_t after = ~nw32 >> b;
-      const uint32_t len = after ? (uint32_t)__ffs(after) - 1 : 32u;
-      const uint32_t o = threadIdx.x * 16u + b;
+      // token length from the 64-byte non-whitespace mask, if it ends there
+      const uint64_t after = ~nw64 >> b;
+      const uint32_t len = after ? (uint32_t)__ffsll((long long)after) - 1 : 64u;
+      const uint32_t o = threadIdx.x * 32u + b;
       uint64_t v = 0;
       bool ok;
       if (len <= 8) {
@@ -379,7 +386,7 @@ int wah_parse_text(const void* d_text, uint64_t bytes, uint32_t* d_values, uint6
   in.text = static_cast<const unsigned char*>(d_text);
   in.bytes = bytes;
   const uint64_t rb = ceil_div(bytes ? bytes : 1, ranges);
-  in.range_bytes = ceil_div(rb, kPStep) * kPStep;
+  in.range_bytes = ceil_div(rb, kPEStep) * kPEStep;
   in.ranges = ranges;
   k_parse_count<<<ranges, kPThreads, 0, s>>>(in, rng);
   k_parse_scan<<<1, kPScanThreads, 0, s>>>(rng, ranges, ctrl);
