@@ -481,6 +481,10 @@ __device__ __forceinline__ void build_emit(const G& g, const uint32_t* __restric
       pc = c;
     }
     const uint32_t nk = __popc(vheadm);
+    // A warp whose every thread has 16 heads, each with a fill, and no key
+    // start (most warps of a column whose keys are spread over its chunks)
+    // writes its words in a fixed pattern: fill, literal, row by row.
+    const bool fast = __all_sync(0xffffffffu, full && nw == 2u * kBuildItems && vheadm == 0);
 
     // Literals: the rows after this thread's last row that continue its last
     // segment (from the window), then a reverse segmented OR over its rows.
@@ -499,11 +503,17 @@ __device__ __forceinline__ void build_emit(const G& g, const uint32_t* __restric
       }
     }
     uint32_t lits[kBuildItems];
+    if (fast) {  // every row is its own segment; the last one takes the continuation
 #pragma unroll
-    for (int j = kBuildItems - 1; j >= 0; --j) {
-      if (first + j < exist) acc |= 1u << bt[j];  // rows past n add nothing
-      lits[j] = acc;
-      if (headm & (1u << j)) acc = 0x80000000u;
+      for (int j = 0; j < kBuildItems; ++j) lits[j] = 0x80000000u | (1u << bt[j]);
+      lits[kBuildItems - 1] |= acc;
+    } else {
+#pragma unroll
+      for (int j = kBuildItems - 1; j >= 0; --j) {
+        if (first + j < exist) acc |= 1u << bt[j];  // rows past n add nothing
+        lits[j] = acc;
+        if (headm & (1u << j)) acc = 0x80000000u;
+      }
     }
 
     // Tile scan of (words, keys); the warp totals are read before the
@@ -516,16 +526,24 @@ __device__ __forceinline__ void build_emit(const G& g, const uint32_t* __restric
 
     uint32_t pw = my_prefix & kPackMask;
     uint32_t pk = my_prefix >> kPackShift;
+    if (fast) {
 #pragma unroll
-    for (int j = 0; j < kBuildItems; ++j) {
-      if (headm & (1u << j)) {
-        if (vheadm & (1u << j)) {
-          if (!derive) sm.keys[skew(pk)] = v[j];
-          sm.offs[skew(pk)] = run_w + pw;
-          ++pk;
+      for (int j = 0; j < kBuildItems; ++j) {
+        words[skew(pw + 2 * j)] = fills[j];
+        words[skew(pw + 2 * j + 1)] = lits[j];
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < kBuildItems; ++j) {
+        if (headm & (1u << j)) {
+          if (vheadm & (1u << j)) {
+            if (!derive) sm.keys[skew(pk)] = v[j];
+            sm.offs[skew(pk)] = run_w + pw;
+            ++pk;
+          }
+          if (fills[j]) words[skew(pw++)] = fills[j];
+          words[skew(pw++)] = lits[j];
         }
-        if (fills[j]) words[skew(pw++)] = fills[j];
-        words[skew(pw++)] = lits[j];
       }
     }
     __syncthreads();

@@ -78,6 +78,34 @@ struct DecodeAct {
   }
 };
 
+// Decode to row ids only (with optional per-key first positions): no key
+// values are read, and the bounds are checked once per literal word.
+struct DecodeRowsAct {
+  uint32_t* rows;
+  uint32_t* key_rows;  // [K] or nullptr
+  uint64_t n;
+  uint32_t* status;
+  static constexpr bool kNeedsValue = false;
+  __device__ __forceinline__ void head(uint32_t key, uint32_t pos) const {
+    if (key_rows) key_rows[key] = pos;
+  }
+  __device__ __forceinline__ void literal(uint32_t, uint32_t chunk, uint32_t bits,
+                                          uint32_t pos) const {
+    const uint64_t base = (uint64_t)chunk * 31u;
+    const uint32_t top = 31u - __clz(bits);  // highest row of the chunk (bits != 0)
+    if (bits == 0 || base + top >= n || (uint64_t)pos + __popc(bits) > n) {
+      if (bits) set_status(status, WAH_ECORRUPT);
+      return;
+    }
+    uint32_t* out = rows + pos;
+    while (bits) {
+      const uint32_t b = __ffs(bits) - 1;
+      bits &= bits - 1;
+      *out++ = (uint32_t)(base + b);
+    }
+  }
+};
+
 // Expand action: OR every literal into a dense chunk array.
 struct ExpandAct {
   uint32_t* dense;
@@ -338,8 +366,15 @@ int wah_decode(const uint32_t* d_keys, const uint32_t* d_offsets, const uint32_t
   cudaError_t e = cudaMemsetAsync(d_status, 0, sizeof(uint32_t), s);
   WalkIn in{d_keys, d_offsets, d_index, keycnt, index_len};
   WalkWs ws = walk_ws(static_cast<unsigned char*>(d_workspace));
-  DecodeAct act{d_keys, d_rows, d_row_values, d_column, d_key_rows, n, d_status};
-  if (e == cudaSuccess) e = enqueue_walk(in, 0u, 0xFFFFFFFFu, ws, act, s, &launches);
+  if (e == cudaSuccess) {
+    if (d_rows && !d_row_values && !d_column) {
+      DecodeRowsAct act{d_rows, d_key_rows, n, d_status};
+      e = enqueue_walk(in, 0u, 0xFFFFFFFFu, ws, act, s, &launches);
+    } else {
+      DecodeAct act{d_keys, d_rows, d_row_values, d_column, d_key_rows, n, d_status};
+      e = enqueue_walk(in, 0u, 0xFFFFFFFFu, ws, act, s, &launches);
+    }
+  }
   if (e == cudaSuccess) {
     k_decode_check<<<1, 32, 0, s>>>(ws.span, n, d_status);
     ++launches;
