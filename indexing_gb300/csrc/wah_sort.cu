@@ -1206,7 +1206,7 @@ __global__ void __launch_bounds__(kSortThreads, ITEMS <= 12 ? 3 : 2)
             }
             rout[g] = sm.out_rids[k];
           } else {
-            set_status(status, WAH_ETIMEOUT);
+            set_status(status, WAH_ECORRUPT);
           }
         }
       }
