@@ -293,6 +293,96 @@ __global__ void __launch_bounds__(kScanThreads) k_walk_scan(WalkAgg* agg, uint32
   if (threadIdx.x == 0) sp->rows = pop_total;
 }
 
+// One tile [t0, t1) of the emit walk, each thread's kQItems words.  kFull:
+// the tile holds kQTile words (16-byte loads where the words are aligned);
+// kHeads: key heads (s_heads[0, nh)) may lie in it.  Both are the same for
+// the whole block, so every thread takes the same instance and the block
+// scans inside line up.  Most tiles are full and hold no key head.
+template <bool kFull, bool kHeads, class Act>
+__device__ __forceinline__ void walk_tile(const WalkIn& in, const Act& act,
+                                          const uint32_t* s_heads, uint32_t nh, uint32_t t0,
+                                          uint32_t t1, uint32_t kcur, uint32_t& chunk_carry,
+                                          uint32_t& pop_carry, Seg* s_seg, uint32_t* s_pop) {
+  const uint32_t p = t0 + threadIdx.x * kQItems;  // this thread's words [p, p + kQItems)
+  uint32_t h0 = 0;  // heads before p
+  if constexpr (kHeads) {
+    uint32_t lo = 0, hi = nh;
+    while (lo < hi) {
+      const uint32_t mid = (lo + hi) >> 1;
+      if (s_heads[mid] < p) lo = mid + 1;
+      else hi = mid;
+    }
+    h0 = lo;
+  }
+  uint32_t w[kQItems];
+  if (kFull && (reinterpret_cast<uintptr_t>(in.index + t0) & 15) == 0) {
+    const uint4* w4 = reinterpret_cast<const uint4*>(in.index + p);
+#pragma unroll
+    for (int q = 0; q < kQItems / 4; ++q) {
+      const uint4 v = w4[q];
+      w[4 * q + 0] = v.x;
+      w[4 * q + 1] = v.y;
+      w[4 * q + 2] = v.z;
+      w[4 * q + 3] = v.w;
+    }
+  } else {
+#pragma unroll
+    for (int q = 0; q < kQItems; ++q) w[q] = (kFull || p + q < t1) ? in.index[p + q] : 0u;
+  }
+  Seg loc = {0, 0};
+  uint32_t pop = 0;
+  {
+    uint32_t h = h0;
+#pragma unroll
+    for (int q = 0; q < kQItems; ++q) {
+      if (!kFull && p + q >= t1) break;
+      if (kHeads && h < nh && s_heads[h] == p + q) {
+        loc = Seg{1, 0};
+        ++h;
+      }
+      loc.s += chunk_advance(w[q]);
+      pop += lit_rows(w[q]);
+    }
+  }
+  Seg tot;
+  const Seg ex = block_seg_exclusive<kQThreads>(loc, &tot, s_seg);
+  uint32_t pop_tot;
+  const uint32_t pop_ex = block_exclusive_scan<kQThreads>(pop, &pop_tot, s_pop);
+  uint32_t chunk = ex.f ? ex.s : chunk_carry + ex.s;
+  uint32_t pos = pop_carry + pop_ex;
+  // key of word p - 1; a head at p (or later) moves it on before any
+  // literal of the new key, so keys[] is read only for valid keys
+  uint32_t key = kcur + h0;
+  uint32_t value = 0, value_key = kNone;
+  {
+    uint32_t h = h0;
+#pragma unroll
+    for (int q = 0; q < kQItems; ++q) {
+      if (!kFull && p + q >= t1) break;
+      if (kHeads && h < nh && s_heads[h] == p + q) {
+        ++h;
+        ++key;
+        chunk = 0;
+        act.head(key, pos);
+      }
+      const uint32_t x = w[q];
+      if (x & kLitBit) {
+        if (Act::kNeedsValue && key != value_key) {
+          value = in.keys[key];
+          value_key = key;
+        }
+        act.literal(value, chunk, x & 0x7FFFFFFFu, pos);
+        pos += __popc(x & 0x7FFFFFFFu);
+        chunk += 1;
+      } else {
+        chunk += x & kFillMask;
+      }
+    }
+  }
+  chunk_carry = tot.f ? tot.s : chunk_carry + tot.s;
+  pop_carry += pop_tot;
+}
+
 template <class Act>
 __global__ void __launch_bounds__(kQThreads) k_walk_emit(WalkIn in, const Span* sp,
                                                           const WalkAgg* agg, Act act) {
@@ -331,70 +421,17 @@ __global__ void __launch_bounds__(kQThreads) k_walk_emit(WalkIn in, const Span* 
       nh += inside;
       if (inside < (uint32_t)kQThreads) break;
     }
-    // this thread's words [p, p + kQItems)
-    const uint32_t p = t0 + threadIdx.x * kQItems;
-    uint32_t lo = 0, hi = nh;  // heads before p
-    while (lo < hi) {
-      const uint32_t mid = (lo + hi) >> 1;
-      if (s_heads[mid] < p) lo = mid + 1;
-      else hi = mid;
+    if (t1 - t0 == kQTile) {
+      if (nh == 0)
+        walk_tile<true, false>(in, act, s_heads, nh, t0, t1, kcur, chunk_carry, pop_carry,
+                               s_seg, s_pop);
+      else
+        walk_tile<true, true>(in, act, s_heads, nh, t0, t1, kcur, chunk_carry, pop_carry, s_seg,
+                              s_pop);
+    } else {
+      walk_tile<false, true>(in, act, s_heads, nh, t0, t1, kcur, chunk_carry, pop_carry, s_seg,
+                             s_pop);
     }
-    const uint32_t h0 = lo;
-    uint32_t w[kQItems];
-#pragma unroll
-    for (int q = 0; q < kQItems; ++q) w[q] = p + q < t1 ? in.index[p + q] : 0u;
-    Seg loc = {0, 0};
-    uint32_t pop = 0;
-    {
-      uint32_t h = h0;
-#pragma unroll
-      for (int q = 0; q < kQItems; ++q) {
-        if (p + q >= t1) break;
-        if (h < nh && s_heads[h] == p + q) {
-          loc = Seg{1, 0};
-          ++h;
-        }
-        loc.s += chunk_advance(w[q]);
-        pop += lit_rows(w[q]);
-      }
-    }
-    Seg tot;
-    const Seg ex = block_seg_exclusive<kQThreads>(loc, &tot, s_seg);
-    uint32_t pop_tot;
-    const uint32_t pop_ex = block_exclusive_scan<kQThreads>(pop, &pop_tot, s_pop);
-    uint32_t chunk = ex.f ? ex.s : chunk_carry + ex.s;
-    uint32_t pos = pop_carry + pop_ex;
-    // key of word p - 1; a head at p (or later) moves it on before any
-    // literal of the new key, so keys[] is read only for valid keys
-    uint32_t key = kcur + h0;
-    uint32_t value = 0, value_key = kNone;
-    {
-      uint32_t h = h0;
-#pragma unroll
-      for (int q = 0; q < kQItems; ++q) {
-        if (p + q >= t1) break;
-        if (h < nh && s_heads[h] == p + q) {
-          ++h;
-          ++key;
-          chunk = 0;
-          act.head(key, pos);
-        }
-        const uint32_t x = w[q];
-        if (x & kLitBit) {
-          if (Act::kNeedsValue && key != value_key) {
-            value = in.keys[key];
-            value_key = key;
-          }
-          act.literal(value, chunk, x & 0x7FFFFFFFu, pos);
-          pos += __popc(x & 0x7FFFFFFFu);
-          chunk += 1;
-        } else {
-          chunk += x & kFillMask;
-        }
-      }
-    }
-    chunk_carry = tot.f ? tot.s : chunk_carry + tot.s;
-    pop_carry += pop_tot;
     kcur += nh;
     __syncthreads();  // s_heads is rewritten by the next tile
   }

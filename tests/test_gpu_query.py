@@ -72,6 +72,22 @@ def test_decode_matches_oracle(wah, name, v):
         assert u32(d["rows"])[starts[i]:end].tolist() == ones, f"{name}: key {i}"
 
 
+@pytest.mark.parametrize("name,v", list(columns()))
+def test_decode_rows_only_matches_oracle(wah, name, v):
+    """Row ids alone (and with each key's first position) take the decoder's
+    lean path: the same row ids as the oracle's stable sort."""
+    n = v.size
+    idx = wah.build_index(v)
+    sv, sr = O.sort_rids_by_value(v)
+    d = wah.decode(idx, n)
+    assert np.array_equal(u32(d["rows"]), sr), f"{name}: row ids"
+    d2 = wah.decode(idx, n, rows=True, key_rows=True)
+    assert np.array_equal(u32(d2["rows"]), sr), f"{name}: row ids (with key starts)"
+    starts = u32(d2["key_rows"])
+    keys = u32(idx.keys)
+    assert np.array_equal(starts, np.searchsorted(sv, keys)), f"{name}: key row starts"
+
+
 def test_decode_empty_and_launches(wah):
     idx = wah.build_index(np.zeros(0, np.uint32))
     d = wah.decode(idx, 0, rows=True, column=True)
@@ -89,6 +105,9 @@ def test_decode_reports_wrong_row_count(wah):
     for n in (9_000, 12_000):
         with pytest.raises(wah.WahError) as e:
             wah.decode(idx, n, rows=True, column=True)
+        assert e.value.status == wah.WAH_ECORRUPT
+        with pytest.raises(wah.WahError) as e:  # the row-ids-only path
+            wah.decode(idx, n)
         assert e.value.status == wah.WAH_ECORRUPT
 
 
