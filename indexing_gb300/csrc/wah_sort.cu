@@ -11,17 +11,22 @@
 //
 //   k_digit_histogram  one read of the keys (128-bit loads): the digit-0
 //                      histogram per range, the OR of all keys and the OR of
-//                      their complements
-//   k_sort_plan        trivial digits (every key shares them) skipped, homes
-//                      of each pass
+//                      their complements (one column: also its bin totals,
+//                      and CTA 0 zeroes the result counters)
+//   k_sort_plan        batches: trivial digits (every key shares them)
+//                      skipped, homes of each pass
 //   k_range_count      for digit passes after the first: per-range histogram
 //                      of the digit over the current order (one read of keys);
 //                      in key-start mode also the rows of every 16-bit key
-//   k_key_starts       key-start mode: the first row of every key in the
-//                      sorted order marked in a bit per row, the keys written
-//   k_range_scan       start of every (range, bin) = bin offset (a scan of
-//                      the bins' totals over all ranges) + counts of the same
-//                      bin in earlier ranges
+//   k_range_scan       batches: start of every (range, bin) = bin offset (a
+//                      scan of the bins' totals over all ranges) + counts of
+//                      the same bin in earlier ranges
+//   k_range_scan_one   one column: the same starts, one CTA per bin from the
+//                      bin totals; digit pass 0 also writes the plan and
+//                      zeroes the key counts and key-start bits, and for digit
+//                      pass 1 more CTAs of the same launch run the key starts
+//                      (the first row of every key in the sorted order marked
+//                      in a bit per row, the keys written)
 //   k_radix_scatter    per range, tile after tile: the next tile's keys and
 //                      row ids are fetched by cp.async.bulk into shared memory
 //                      while this one is ranked (warp peer masks, stable per
@@ -31,7 +36,11 @@
 //                      and the later passes may use different tile shapes,
 //                      each over its own ranges; keys between two passes are
 //                      16-bit when every key is below 2^16, and in key-start
-//                      mode the last pass writes row ids only.
+//                      mode the last pass writes row ids only; where pass-0
+//                      ranges are long, the two passes exchange one packed
+//                      word per row instead (scatter_pack0 / scatter_pack1).
+// Every kernel of a one-column build is launched as a programmatic dependent
+// of the one before it (launch_kernel) and waits for it on entry.
 #include <algorithm>
 #include <numeric>
 #include <type_traits>
@@ -487,12 +496,6 @@ __device__ __forceinline__ void key_starts(const G& g, uint32_t block, uint64_t*
   else set_status(c.status, WAH_ECORRUPT);
   if (rank < c.keys_cap) c.keys[rank] = key;
   else set_status(c.status, WAH_EOVERFLOW);
-}
-
-template <class G>
-__global__ void __launch_bounds__(kKeyStartThreads) k_key_starts(G g) {
-  __shared__ uint64_t s_warp[kKeyStartThreads / 32 + 1];
-  key_starts(g, blockIdx.x, s_warp);
 }
 
 // Start of every (range, bin) of one column for one pass: the bin's offset
