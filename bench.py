@@ -196,6 +196,49 @@ def replica_throughput(elapsed_ms: float, rows_per_step: int, steps: int, dist=N
     return max_ms, world * rows_per_step * steps / (max_ms / 1e3)
 
 
+def build_bytes(n: int, card: int, L: int, K: int, tuning: int, sms: int):
+    """Algorithmic bytes of each phase and main kernel of one index build of
+    n rows with `card` possible values (the bound + 1), L index words and K
+    keys, as the library runs it with tuning word `tuning` on `sms` SMs.
+    Returns (bytes by phase/kernel name, digit passes, 16-bit keys between
+    the passes, key-start mode, packed exchange).
+
+    The packed exchange runs when a pass-0 range -- a whole number of tiles
+    of 256 x items rows, SMs x resident scatter CTAs ranges -- holds 2^16 to
+    2^24 rows (or the word forces it), as launch_sort_one decides."""
+    passes = max(1, -(-(card - 1).bit_length() // 8))
+    mid16 = passes == 2
+    derive = mid16 and card > 256
+    rows_in = 4 * n + n // 8 if derive else 8 * n
+    alg = {"histogram": 4 * n, "plan": 0,
+           "emit": rows_in + 4 * L + (4 * K if derive else 8 * K)}
+    alg["build"] = alg["emit"] + rows_in  # the build count reads the same rows first
+    items = tuning & 0xFF
+    ranges = sms * {8: 4, 12: 3, 16: 2}.get(items, 2)
+    quantum = 256 * max(items, 1)
+    range_rows = max(-(-(-(-n // ranges)) // quantum) * quantum, quantum)
+    packed = bool(derive and range_rows < (1 << 24)
+                  and (range_rows >= (1 << 16) or tuning & 0x400))
+    for p in range(4):
+        if p >= passes:
+            a = 0
+        elif packed:
+            a = 8 * n  # pass 0: key in, packed word out; pass 1: packed word in, rid out
+        elif derive:
+            a = 10 * n  # pass 0: key in, 16-bit key + rid out; pass 1: both in, rid out
+        elif mid16:
+            a = 10 * n if p == 0 else 14 * n
+        else:
+            a = 12 * n if p == 0 else 16 * n
+        alg[f"pass{p}"] = a
+        alg[f"scatter{p}"] = a
+    if derive:
+        alg["pass0"] += n // 8  # the range scan zeroes the key-start bits
+        # the count over the pass-0 output; the key starts write the keys
+        alg["pass1"] += (4 * n if packed else 2 * n) + 4 * K
+    return alg, passes, mid16, derive, packed
+
+
 def time_events(fn, steps, torch, stream):
     """Mean ms of fn() over steps, CUDA events on `stream`."""
     a = torch.cuda.Event(enable_timing=True)
@@ -1235,39 +1278,9 @@ def main():
     # (count + scan + kernel) and its main kernel are credited the same
     # bytes, except the pass-1 count and the build count; the roofline is
     # taken on the longest single kernel.
-    passes = max(1, -(-(card - 1).bit_length() // 8))
-    mid16 = passes == 2
-    derive = mid16 and card > 256
-    rows_in = 4 * n + n // 8 if derive else 8 * n
-    alg = {"histogram": 4 * n, "plan": 0,
-           "emit": rows_in + 4 * L + (4 * K if derive else 8 * K)}
-    alg["build"] = alg["emit"] + rows_in  # the build count reads the same rows first
-    # the packed exchange runs when a pass-0 range (a whole number of
-    # 256 x items-row tiles, SMs x resident CTAs ranges) holds 2^16..2^24 rows
-    tuning = int(lib.wah_get_tuning())
-    items = tuning & 0xFF
-    ranges = torch.cuda.get_device_properties(dev).multi_processor_count * \
-        {8: 4, 12: 3, 16: 2}.get(items, 2)
-    quantum = 256 * max(items, 1)
-    range_rows = max(-(-(-(-n // ranges)) // quantum) * quantum, quantum)
-    packed = derive and range_rows < (1 << 24) and (range_rows >= (1 << 16) or tuning & 0x400)
-    for p in range(4):
-        if p >= passes:
-            a = 0
-        elif packed:
-            a = 8 * n  # pass 0: key in, packed word out; pass 1: packed word in, rid out
-        elif derive:
-            a = 10 * n  # pass 0: key in, 16-bit key + rid out; pass 1: both in, rid out
-        elif mid16:
-            a = 10 * n if p == 0 else 14 * n
-        else:
-            a = 12 * n if p == 0 else 16 * n
-        alg[f"pass{p}"] = a
-        alg[f"scatter{p}"] = a
-    if derive:
-        alg["pass0"] += n // 8  # the range scan zeroes the key-start bits
-        # the count over the pass-0 output; the key starts write the keys
-        alg["pass1"] += (4 * n if packed else 2 * n) + 4 * K
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    alg, passes, mid16, derive, packed = build_bytes(n, card, L, K, int(lib.wah_get_tuning()),
+                                                     sms)
     # DRAM bytes per row of each kernel (dram__bytes_read.sum +
     # dram__bytes_write.sum, one ncu capture of a 67,108,864-row uniform
     # 16-bit column with the same tile shape); traffic grows with rows.

@@ -54,3 +54,36 @@ def test_result_fingerprint():
     shifted = offs.copy()
     shifted[1] += 1
     assert h(keys, shifted, index) != base
+
+
+def test_build_bytes_follows_the_library_geometry():
+    """The benchmark's algorithmic bytes per phase: the 268,435,456-row
+    16-bit column exchanges packed words (8 B/row per digit pass, 32.4n +
+    4L + 8K in all), the 1,048,576-row column keeps the 16-bit exchange, a
+    one-byte column takes one pass, and full 32-bit keys four."""
+    n, sms = 268_435_456, 152
+    L, K = 2 * n - 1000, 65_536
+    alg, passes, mid16, derive, packed = bench.build_bytes(n, 65_536, L, K, 524, sms)
+    assert (passes, mid16, derive, packed) == (2, True, True, True)
+    assert alg["scatter0"] == alg["scatter1"] == 8 * n
+    assert alg["pass2"] == alg["pass3"] == 0
+    total = sum(alg[p] for p in ("histogram", "pass0", "pass1", "build"))
+    assert total == 4 * n + (8 * n + n // 8) + (8 * n + 4 * n + 4 * K) + \
+        2 * (4 * n + n // 8) + 4 * L + 4 * K
+    assert abs((total - 4 * L - 8 * K) / n - 32.375) < 1e-9
+    # C1: pass-0 ranges of one 2,048- or 3,072-row tile, below 2^16 rows
+    n1 = 1 << 20
+    for tuning in (8, 524):
+        alg1, _, _, derive1, packed1 = bench.build_bytes(n1, 65_536, 2 * n1, K, tuning, sms)
+        assert derive1 and not packed1
+        assert alg1["scatter0"] == alg1["scatter1"] == 10 * n1
+    # the packed exchange forced by the tuning word
+    assert bench.build_bytes(n1, 65_536, 2 * n1, K, 524 | 0x400, sms)[4]
+    # values below 256: one pass, no key starts
+    alg2, passes2, _, derive2, packed2 = bench.build_bytes(n, 256, n, 256, 524, sms)
+    assert (passes2, derive2, packed2) == (1, False, False)
+    assert alg2["scatter0"] == 12 * n and alg2["scatter1"] == 0
+    # full 32-bit keys: four passes of 32-bit keys and row ids
+    alg3, passes3, mid3, derive3, _ = bench.build_bytes(n, 1 << 32, n, n, 524, sms)
+    assert (passes3, mid3, derive3) == (4, False, False)
+    assert [alg3[f"scatter{p}"] for p in range(4)] == [12 * n, 16 * n, 16 * n, 16 * n]
