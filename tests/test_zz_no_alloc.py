@@ -74,6 +74,12 @@ def test_noalloc_matches_wah_build_twice(bound):
         assert a[1] == b[1]
         for x, y in zip(a[2:], b[2:]):
             assert np.array_equal(x, y)
+        # and word for word what the oracle builds
+        from oracle import oracle as O
+        o = O.build(v)
+        assert b[1] == o.merged
+        assert np.array_equal(b[2], o.keys) and np.array_equal(b[3], o.offsets)
+        assert np.array_equal(b[4], o.index)
 
 
 def test_noalloc_refuses_oversize():
