@@ -39,6 +39,29 @@ def test_every_declared_symbol_is_exported(lib):
         assert name in _lib.SIGNATURES, f"{name} has no ctypes signature"
 
 
+def declared_parameter_counts():
+    """Parameters of every function the header declares (void -> 0)."""
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    out = {}
+    for m in re.finditer(r"^[A-Za-z_][\w\s\*]*?\b(wah_\w+)\s*\(([^;]*?)\)\s*;", text,
+                         flags=re.M | re.S):
+        params = " ".join(m.group(2).split())
+        out[m.group(1)] = 0 if params in ("", "void") else params.count(",") + 1
+    return out
+
+
+def test_ctypes_signatures_match_the_header():
+    """Every binding in the Python signature table takes as many arguments as
+    the header declares, so a parameter added on one side only fails here
+    on the CPU instead of corrupting a call on the GPU."""
+    counts = declared_parameter_counts()
+    assert set(counts) == set(declared_functions())
+    for name, n in counts.items():
+        argtypes = _lib.SIGNATURES[name][0]
+        assert len(argtypes) == n, f"{name}: header {n} parameters, ctypes {len(argtypes)}"
+
+
 def test_strerror(lib):
     assert lib.wah_strerror(0) == b"ok"
     assert b"range" in lib.wah_strerror(5)
